@@ -1,0 +1,182 @@
+/*
+ * ns_gb300.h -- C ABI of the GB300 (sm_103a) time-step library for the
+ * mathe1s/NavierStokes aeroacoustic solver.
+ *
+ * The library replaces the reference's LDDRK stage loop, rk_euler
+ * (rk.f90:12-75), and everything it calls: the DRP derivatives with their
+ * boundary closures and 1-D metrics (diff.f90, derivs.f90), the transport
+ * law (coefficients.f90), the primitive Navier-Stokes right-hand side
+ * (rhs.f90, eqeuler.f90), the stage update and buffer damping (rk.f90), the
+ * in-place 13-point selective filter (filtering.f90) and the boundary
+ * conditions (cc.f90).  The inputs the reference reads from module `global`
+ * (global.f90) are passed once in ns_params; the state U stays resident on
+ * the GPU between calls.
+ *
+ * Conventions: plain C types only; every entry point returns an ns_status
+ * (0 = NS_OK) and never aborts the process; ns_last_error() gives the text
+ * of the last failure on a context.  One context per host thread; calls on
+ * one context are not re-entrant.
+ */
+#ifndef NS_GB300_H
+#define NS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NS_ABI_VERSION 1
+
+#if defined(__GNUC__)
+#define NS_API __attribute__((visibility("default")))
+#else
+#define NS_API
+#endif
+
+typedef enum ns_status {
+    NS_OK = 0,
+    NS_ERR_PARAM = 1,       /* invalid argument or unsupported size */
+    NS_ERR_CUDA = 2,        /* a CUDA runtime call failed */
+    NS_ERR_OOM = 3,         /* device or host allocation failed */
+    NS_ERR_NONFINITE = 4,   /* the state holds NaN/Inf (ns_check_finite) */
+    NS_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up */
+    NS_ERR_STATE = 6,       /* call out of order (e.g. step before set_state) */
+    NS_ERR_UNSUPPORTED = 7  /* feature not available in this build/context */
+} ns_status;
+
+/* Host array layouts accepted by ns_set_state/ns_get_state. */
+enum {
+    NS_LAYOUT_FORTRAN = 0, /* U(nk,imax,jmax), column-major: the reference's
+                              own array (euler.f90:107) */
+    NS_LAYOUT_SOA = 1      /* U[k][j][i], i fastest: one plane per variable */
+};
+
+/* Arithmetic of the stage loop. */
+enum {
+    NS_PREC_FP64 = 0,  /* plain FP64, the reference's arithmetic */
+    NS_PREC_SPLIT = 1  /* FP64 mean flow + FP32 perturbation state */
+};
+
+/* Acoustic source of rk.f90:171-193. */
+enum {
+    NS_SRC_NONE = 0,
+    NS_SRC_GAUSSIAN = 1, /* s = amplitude*sin(wf*(iter+c)*dt)
+                                *exp(-ln2*((m-m_pt)^2+(n-n_pt)^2)/r0^2) */
+    NS_SRC_FIELD = 2     /* s = sin(wf*(iter+c)*dt) * src_field(i,j) */
+};
+
+/* Metric application of diff.f90:276-350. */
+enum {
+    NS_METRIC_BANDS = 0,   /* reference: meshx/meshy multiply derivatives only
+                              inside the D-wide buffer bands */
+    NS_METRIC_EVERYWHERE = 1 /* meshx(i)/meshy(j) multiply every derivative
+                                (stretched-grid cases) */
+};
+
+/*
+ * Everything rk_euler reads from module `global` (global.f90) and from the
+ * setup routines init_dados/init_variables (init.f90:56-418).  The library
+ * copies what it needs during ns_create; the caller may free the arrays
+ * afterwards.
+ */
+typedef struct ns_params {
+    int32_t abi_version;   /* = NS_ABI_VERSION */
+    int32_t imax, jmax;    /* grid points, >= 13 each (global.f90:13) */
+    int32_t nk;            /* 5 = (rho,u,v,p,psi) as the reference
+                              (global.f90:19); 4 = without the passive psi */
+    int32_t D;             /* buffer width, 0 <= 2*D <= min(imax,jmax) */
+    int32_t inviscid;      /* 1: Euler (1/Re = 0); 0: Navier-Stokes */
+    int32_t metric_mode;   /* NS_METRIC_* */
+    int32_t precision;     /* NS_PREC_* */
+    int32_t source_mode;   /* NS_SRC_* */
+    int32_t device;        /* CUDA device ordinal */
+    int32_t ub_layout;     /* layout of Ub: NS_LAYOUT_* */
+    int32_t reserved0;
+    double dt, dm, dn;     /* time step, grid steps (init.f90:68-70) */
+    double sigmaf;         /* filter strength (dados.in &grid sigmaf) */
+    double gamma;          /* ratio of specific heats (init.f90:361) */
+    double Re, Pr;         /* Reynolds, Prandtl numbers (&flow) */
+    double Tref;           /* reference temperature (&flow) */
+    /* Transport fit exp(A*ln(x)+B/x+C/x^2+D), x = Tref*T, for mu and k
+     * (coefficients.f90:27-59; N2 values in SPECIE_N, :113-123). */
+    double A_mi, B_mi, C_mi, D_mi;
+    double A_k, B_k, C_k, D_k;
+    /* source parameters (&freq), used by NS_SRC_GAUSSIAN / NS_SRC_FIELD */
+    double amplitude, wf, m_pt, n_pt, r0;
+    const double *m;       /* [imax] x coordinates (init.f90:104-107) */
+    const double *n;       /* [jmax] y coordinates (init.f90:113-115) */
+    const double *meshx;   /* [imax] x metric (init.f90:123-137) */
+    const double *meshy;   /* [jmax] y metric (init.f90:139-153) */
+    const double *sigmax;  /* [imax] buffer damping (init.f90:158-181) */
+    const double *sigmay;  /* [jmax] buffer damping (init.f90:183-206) */
+    const double *rhob;    /* [jmax] inflow density (cc.f90:23) */
+    const double *psib;    /* [jmax] inflow scalar (cc.f90:27), nk = 5 */
+    const double *Ub;      /* base flow, nk*imax*jmax in ub_layout
+                              (init.f90:392-404) */
+    const double *src_field; /* [imax*jmax], i fastest (NS_SRC_FIELD) */
+} ns_params;
+
+typedef struct ns_ctx ns_ctx;
+
+/* Library/ABI identification. */
+NS_API int ns_abi_version(void);
+NS_API const char *ns_build_info(void);
+
+/* Fills the defaults the reference fixes in code: gamma = 1.4
+ * (init.f90:361), the N2 transport fit (coefficients.f90:113-123),
+ * Tref = 273.15, nk = 5, metric bands, FP64.  Sizes and arrays are zeroed. */
+NS_API int ns_params_init(ns_params *p);
+
+/* Validates p, allocates the device state and work arrays and uploads the
+ * setup arrays.  Replaces the module state that init_read/init_dados/
+ * init_variables leave for rk_euler (init.f90:10-418). */
+NS_API int ns_create(const ns_params *p, ns_ctx **out);
+NS_API void ns_destroy(ns_ctx *ctx);
+NS_API const char *ns_last_error(const ns_ctx *ctx);  /* ctx may be NULL */
+
+/* Host <-> device state transfer (synchronous).  U holds nk*imax*jmax
+ * doubles in `layout`. */
+NS_API int ns_set_state(ns_ctx *ctx, const double *U, int layout);
+NS_API int ns_get_state(ns_ctx *ctx, double *U, int layout);
+
+/* Advances the resident state by nsteps calls of rk_euler (rk.f90:12) with
+ * iter = iter0, iter0+1, ...: six LDDRK stages each.  Asynchronous with
+ * respect to the host (ordered on the context's stream); launch errors are
+ * returned at once, execution errors by the next synchronising call. */
+NS_API int ns_step(ns_ctx *ctx, int iter0, int nsteps);
+NS_API int ns_synchronize(ns_ctx *ctx);
+
+/* The drop-in for one call `call rk_euler(U,t,iter,nk)` (euler.f90:130,
+ * rk.f90:12): host U in the reference layout U(nk,imax,jmax) is uploaded,
+ * advanced one step and written back.  t is unused, as in the reference. */
+NS_API int ns_rk_euler(ns_ctx *ctx, double *U, double t, int iter, int nk);
+
+/* Reads U(1..nk) at np points (1-based i, j) into out[np*nk] (point-major):
+ * the probe writes of euler.f90:156-161 without a full download. */
+NS_API int ns_get_probes(ns_ctx *ctx, int np, const int32_t *pi, const int32_t *pj,
+                  double *out);
+
+/* Scans the state for NaN/Inf; sets *nonfinite to the count found and
+ * returns NS_ERR_NONFINITE when it is non-zero. */
+NS_API int ns_check_finite(ns_ctx *ctx, int64_t *nonfinite);
+
+/* Stream the context enqueues on (a cudaStream_t, 0 = the context's own). */
+NS_API int ns_set_stream(ns_ctx *ctx, void *stream);
+NS_API int ns_get_stream(ns_ctx *ctx, void **stream);
+
+/* Device pointer of the resident SoA state: plane k of variable k+1 starts
+ * at *dptr + k*jmax*pitch, row j at + j*pitch (pitch in elements).  For
+ * zero-copy views from PyTorch; valid until ns_destroy. */
+NS_API int ns_state_device(ns_ctx *ctx, void **dptr, int64_t *pitch);
+
+/* Number of kernel launches one ns_step(…,1) enqueues, and the filter
+ * warm-up length used for the chunked recurrences. */
+NS_API int ns_step_launches(ns_ctx *ctx, int *launches);
+NS_API int ns_filter_warmup(ns_ctx *ctx, int *warmup);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NS_GB300_H */

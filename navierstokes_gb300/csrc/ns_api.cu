@@ -1,0 +1,642 @@
+// ns_api.cu -- host side of the C ABI declared in include/ns_gb300.h.
+//
+// Builds, once per context, everything rk_euler (rk.f90:12-75) reads from
+// module `global`: the per-line DRP coefficient tables with 1/dm, 1/dn and
+// the metric folded in (diff.f90:40-350, coefficients init.f90:286-338), the
+// filter coefficient sets (filtering.f90:25-31, :54-66, :114-120), the
+// LDDRK tables (rk.f90:27-46), the transport reference values
+// (coefficients.f90:71-80), the buffer arrays and the base flow.  One step
+// is captured once as a CUDA graph and replayed.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "ns_internal.cuh"
+
+#define NS_STR2(x) #x
+#define NS_STR1(x) NS_STR2(x)
+#define NS_STR_CUDA_VERSION NS_STR1(CUDART_VERSION)
+
+namespace {
+
+thread_local std::string g_last_error;
+
+// DRP coefficients, init.f90:288-338.
+const double kA[3] = {0.770882380518, -0.166705904415, 0.0208431427703};
+const double kA4[7] = {0.049041958000, -0.46884035700, -0.47476091400, 1.27327473700,
+                       -0.51848452600, 0.16613853300,  -0.026369431000};
+const double kA4b[7] = {0.026369431000, -0.16613853300, 0.51848452600, -1.27327473700,
+                        0.47476091400,  0.46884035700,  -0.049041958000};
+const double kA5[7] = {-0.20933762200, -1.08487567600, 2.14777605000, -1.38892832200,
+                       0.76894976600,  -0.28181465000, 0.048230454000};
+const double kA5b[7] = {-0.048230454000, 0.28181465000,  -0.76894976600, 1.38892832200,
+                        -2.14777605000,  1.08487567600, 0.20933762200};
+const double kA6[7] = {-2.19228033900, 4.74861140100, -5.10885191500, 4.46156710400,
+                       -2.83349874100, 1.12832886100, -0.20387637100};
+const double kA6b[7] = {0.20387637100, -1.12832886100, 2.83349874100, -4.46156710400,
+                        5.10885191500, -4.74861140100, 2.19228033900};
+// Selective filter, filtering.f90:54-66 (df(0..6); symmetric).
+const double kDf[7] = {0.190899511506,  -0.171503832236, 0.123632891797, -0.069975429105,
+                       0.029662754736, -0.008520738659, 0.001254597714};
+// Boundary filter dfb(-1..5): REAL(8) literals in x (filtering.f90:25-31),
+// default-REAL (single precision) literals in y (filtering.f90:114-120).
+const double kDfbX[7] = {-0.057717512738, 0.199278374994,  -0.292668277650, 0.244537361546,
+                         -0.134605018019, 0.056184263460, -0.015009191593};
+const double kDfbY[7] = {(double)-0.057717512738f, (double)0.199278374994f,
+                         (double)-0.292668277650f, (double)0.244537361546f,
+                         (double)-0.134605018019f, (double)0.056184263460f,
+                         (double)-0.015009191593f};
+// LDDRK, rk.f90:27-46.
+const double kAlpha[6] = {0.0, -0.737101392796, -1.634740794341,
+                          -0.744739003780, -1.469897351522, -2.813971388035};
+const double kBeta[6] = {0.032918605146, 0.823256998200, 0.381530948900,
+                         0.200092213184, 1.718581042715, 0.27};
+const double kCt[6] = {0.0, 0.032918605146, 0.249351723343,
+                       0.466911705055, 0.582030414044, 0.847252983783};
+// global.f90:38-39
+const double kPe = 1000.0, kAlphaCond = 0.5;
+
+int set_err(ns_ctx *c, int code, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (c) c->err = buf;
+    g_last_error = buf;
+    return code;
+}
+
+int cuda_err(ns_ctx *c, cudaError_t e, const char *what)
+{
+    return set_err(c, NS_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define NS_CUDA(c, call)                                          \
+    do {                                                          \
+        cudaError_t e_ = (call);                                  \
+        if (e_ != cudaSuccess) return cuda_err((c), e_, #call);   \
+    } while (0)
+
+// Per-line coefficient table (see ns::kCoefStride).
+void build_coef(std::vector<double> &tab, int n, double h, const double *mesh, int D,
+                int metric_mode)
+{
+    tab.assign((size_t)n * ns::kCoefStride, 0.0);
+    for (int q = 0; q < n; q++) {
+        double mt = 1.0;
+        if (metric_mode == NS_METRIC_EVERYWHERE)
+            mt = mesh[q];
+        else if (q < D || q >= n - D)
+            mt = mesh[q];
+        double *c = &tab[(size_t)q * ns::kCoefStride];
+        const double *src = nullptr;
+        if (q == 0) src = kA6;
+        else if (q == 1) src = kA5;
+        else if (q == 2) src = kA4;
+        else if (q == n - 3) src = kA4b;
+        else if (q == n - 2) src = kA5b;
+        else if (q == n - 1) src = kA6b;
+        if (src) {
+            for (int z = 0; z < 7; z++) c[z] = src[z] * mt / h;
+        } else {
+            for (int s = 0; s < 3; s++) c[4 + s] = kA[s] * mt / h;
+        }
+    }
+}
+
+ns::FilterCoef make_filter(double sigmaf, const double *dfb)
+{
+    ns::FilterCoef f;
+    std::memset(&f, 0, sizeof f);
+    f.c0 = 1.0 - sigmaf * kDf[0];
+    for (int s = 1; s <= 6; s++) f.m[s] = -sigmaf * kDf[s];
+    f.bm1 = -sigmaf * dfb[0];
+    f.b0 = 1.0 - sigmaf * dfb[1];
+    for (int s = 1; s <= 5; s++) f.b[s] = -sigmaf * dfb[s + 1];
+    return f;
+}
+
+// Warm-up length of the chunked filter recurrence: the number of points
+// after which the response of the homogeneous recurrence
+// e(q) = -sigmaf*sum_{s=1..6} df(s)*e(q-s) to any unit history has fallen
+// below 2^-60 for good, plus a margin.  -1 when it never does (the sweeps
+// then run serially, one chunk per line).
+int filter_warmup(double sigmaf)
+{
+    const int kMax = 4096;
+    const double thresh = std::ldexp(1.0, -60);
+    int worst = 0;
+    for (int u = 0; u < 6; u++) {
+        std::vector<double> e(kMax + 6, 0.0);
+        e[u] = 1.0;
+        int last_big = 0;
+        for (int q = 6; q < kMax + 6; q++) {
+            double v = 0.0;
+            for (int s = 1; s <= 6; s++) v += -sigmaf * kDf[s] * e[q - s];
+            e[q] = v;
+            if (std::fabs(v) >= thresh) last_big = q - 5;
+        }
+        if (last_big >= kMax - 64) return -1;
+        if (last_big > worst) worst = last_big;
+    }
+    int w = worst + 8;
+    if (w < 36) w = 36;
+    return w;
+}
+
+int choose_chunks(int nlines_total, int n, int warm, int target_threads)
+{
+    if (warm < 0) return 1;
+    const int len2 = n - 12;
+    int c = (target_threads + nlines_total - 1) / nlines_total;
+    const int maxc = len2 / (4 * (warm + 6));
+    if (c > maxc) c = maxc;
+    if (c < 1) c = 1;
+    return c;
+}
+
+template <class T>
+int dalloc(ns_ctx *c, T **p, size_t count)
+{
+    cudaError_t e = cudaMalloc((void **)p, count * sizeof(T));
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return set_err(c, NS_ERR_OOM, "cudaMalloc(%zu bytes): %s", count * sizeof(T),
+                       cudaGetErrorString(e));
+    }
+    return NS_OK;
+}
+
+void free_all(ns_ctx *c)
+{
+    if (c->step_exec) cudaGraphExecDestroy(c->step_exec);
+    double *bufs[] = {c->U,    c->U2,   c->W,     c->dudm, c->dudn, c->aux,
+                      c->Ubase, c->src, c->xcoef, c->ycoef, c->sigx, c->sigy,
+                      c->rhob, c->psib, c->stage_sin, c->probe_buf};
+    for (double *b : bufs)
+        if (b) cudaFree(b);
+    if (c->d_iter) cudaFree(c->d_iter);
+    if (c->d_count) cudaFree(c->d_count);
+    if (c->probe_idx) cudaFree(c->probe_idx);
+    if (c->own_stream) cudaStreamDestroy(c->own_stream);
+}
+
+int validate(const ns_params *p)
+{
+    if (!p) return set_err(nullptr, NS_ERR_PARAM, "params is NULL");
+    if (p->abi_version != NS_ABI_VERSION)
+        return set_err(nullptr, NS_ERR_PARAM, "abi_version %d, library is %d", p->abi_version,
+                       NS_ABI_VERSION);
+    if (p->imax < 13 || p->jmax < 13)
+        return set_err(nullptr, NS_ERR_PARAM, "imax=%d jmax=%d: both must be >= 13", p->imax,
+                       p->jmax);
+    if ((long long)p->imax * p->jmax > (1LL << 31))
+        return set_err(nullptr, NS_ERR_PARAM, "grid of %lld points is too large",
+                       (long long)p->imax * p->jmax);
+    if (p->nk != 4 && p->nk != 5) return set_err(nullptr, NS_ERR_PARAM, "nk=%d: must be 4 or 5", p->nk);
+    if (p->D < 0 || 2 * p->D > p->imax || 2 * p->D > p->jmax)
+        return set_err(nullptr, NS_ERR_PARAM, "D=%d: need 0 <= 2*D <= min(imax,jmax)", p->D);
+    if (p->metric_mode != NS_METRIC_BANDS && p->metric_mode != NS_METRIC_EVERYWHERE)
+        return set_err(nullptr, NS_ERR_PARAM, "metric_mode=%d", p->metric_mode);
+    if (p->precision != NS_PREC_FP64)
+        return set_err(nullptr, NS_ERR_UNSUPPORTED, "precision=%d is not available", p->precision);
+    if (p->source_mode < NS_SRC_NONE || p->source_mode > NS_SRC_FIELD)
+        return set_err(nullptr, NS_ERR_PARAM, "source_mode=%d", p->source_mode);
+    if (!(p->dt > 0) || !(p->dm > 0) || !(p->dn > 0) || !(p->gamma > 1.0))
+        return set_err(nullptr, NS_ERR_PARAM, "dt, dm, dn must be > 0 and gamma > 1");
+    if (!p->inviscid && (!(p->Re > 0) || !(p->Pr > 0) || !(p->Tref > 0)))
+        return set_err(nullptr, NS_ERR_PARAM, "viscous case needs Re, Pr, Tref > 0");
+    if (!p->meshx || !p->meshy || !p->sigmax || !p->sigmay || !p->rhob || !p->Ub)
+        return set_err(nullptr, NS_ERR_PARAM, "meshx, meshy, sigmax, sigmay, rhob, Ub are required");
+    if (p->nk == 5 && !p->psib) return set_err(nullptr, NS_ERR_PARAM, "psib is required for nk=5");
+    if (p->source_mode == NS_SRC_GAUSSIAN && (!p->m || !p->n || !(p->r0 != 0.0)))
+        return set_err(nullptr, NS_ERR_PARAM, "gaussian source needs m, n and r0 != 0");
+    if (p->source_mode == NS_SRC_FIELD && !p->src_field)
+        return set_err(nullptr, NS_ERR_PARAM, "field source needs src_field");
+    if (p->ub_layout != NS_LAYOUT_FORTRAN && p->ub_layout != NS_LAYOUT_SOA)
+        return set_err(nullptr, NS_ERR_PARAM, "ub_layout=%d", p->ub_layout);
+    return NS_OK;
+}
+
+// Copies an nk-variable host field in `layout` into device planes.
+int upload_field(ns_ctx *c, const double *h, int layout, double *dplanes)
+{
+    const ns::Dims &d = c->d;
+    const size_t row = (size_t)d.imax * sizeof(double);
+    if (layout == NS_LAYOUT_SOA) {
+        NS_CUDA(c, cudaMemcpy2DAsync(dplanes, d.pitch * sizeof(double), h, row, row,
+                                     (size_t)d.jmax * d.nk, cudaMemcpyHostToDevice, c->stream));
+    } else if (layout == NS_LAYOUT_FORTRAN) {
+        // stage the raw array in the scratch state buffer, then scatter
+        double *stage = (dplanes == c->U2) ? c->dudm : c->U2;
+        NS_CUDA(c, cudaMemcpyAsync(stage, h, (size_t)d.nk * d.imax * d.jmax * sizeof(double),
+                                   cudaMemcpyHostToDevice, c->stream));
+        NS_CUDA(c, ns::launch_aos_to_soa(stage, dplanes, d, c->stream));
+    } else {
+        return set_err(c, NS_ERR_PARAM, "layout=%d", layout);
+    }
+    return NS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ns_abi_version(void) { return NS_ABI_VERSION; }
+
+const char *ns_build_info(void)
+{
+    return "ns_gb300 FP64 stage kernels, sm_103a, CUDA " NS_STR_CUDA_VERSION;
+}
+
+int ns_params_init(ns_params *p)
+{
+    if (!p) return NS_ERR_PARAM;
+    std::memset(p, 0, sizeof *p);
+    p->abi_version = NS_ABI_VERSION;
+    p->nk = 5;
+    p->metric_mode = NS_METRIC_BANDS;
+    p->precision = NS_PREC_FP64;
+    p->source_mode = NS_SRC_NONE;
+    p->ub_layout = NS_LAYOUT_FORTRAN;
+    p->gamma = 1.4;           // init.f90:361
+    p->Tref = 273.15;         // dados.in &flow Tref
+    p->Pr = 0.71;             // dados.in &flow Pr
+    p->Re = 10000.0;          // dados.in &flow Re
+    p->sigmaf = 0.1;          // dados.in &grid sigmaf
+    // SPECIE_N, coefficients.f90:113-123
+    p->A_mi = 0.62526577;
+    p->B_mi = -31.779652;
+    p->C_mi = -1640.7913;
+    p->D_mi = 1.7454992;
+    p->A_k = 0.85372829;
+    p->B_k = 105.18665;
+    p->C_k = -12229.753;
+    p->D_k = 0.48299104;
+    return NS_OK;
+}
+
+const char *ns_last_error(const ns_ctx *ctx)
+{
+    if (ctx && !ctx->err.empty()) return ctx->err.c_str();
+    return g_last_error.c_str();
+}
+
+int ns_create(const ns_params *p, ns_ctx **out)
+{
+    if (!out) return set_err(nullptr, NS_ERR_PARAM, "out is NULL");
+    *out = nullptr;
+    int rc = validate(p);
+    if (rc != NS_OK) return rc;
+
+    ns_ctx *c = new (std::nothrow) ns_ctx();
+    if (!c) return set_err(nullptr, NS_ERR_OOM, "host allocation failed");
+    c->p = *p;
+    c->dev = p->device;
+    cudaError_t e = cudaSetDevice(c->dev);
+    if (e != cudaSuccess) {
+        rc = cuda_err(c, e, "cudaSetDevice");
+        delete c;
+        return rc;
+    }
+    e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        rc = cuda_err(c, e, "cudaStreamCreate");
+        delete c;
+        return rc;
+    }
+    c->stream = c->own_stream;
+
+    ns::Dims &d = c->d;
+    d.imax = p->imax;
+    d.jmax = p->jmax;
+    d.nk = p->nk;
+    d.D = p->D;
+    d.pitch = (p->imax + 31) / 32 * 32;
+    d.plane = (long long)d.pitch * d.jmax;
+    c->visc = !p->inviscid;
+    const size_t P = (size_t)d.plane, nk = (size_t)d.nk;
+
+#define NS_TRY(x)                     \
+    do {                              \
+        rc = (x);                     \
+        if (rc != NS_OK) goto fail;   \
+    } while (0)
+    NS_TRY(dalloc(c, &c->U, nk * P));
+    NS_TRY(dalloc(c, &c->U2, nk * P));
+    NS_TRY(dalloc(c, &c->W, nk * P));
+    NS_TRY(dalloc(c, &c->dudm, nk * P));
+    NS_TRY(dalloc(c, &c->dudn, nk * P));
+    NS_TRY(dalloc(c, &c->aux, (size_t)ns::AUX_COUNT * P));
+    NS_TRY(dalloc(c, &c->Ubase, nk * P));
+    NS_TRY(dalloc(c, &c->xcoef, (size_t)d.imax * ns::kCoefStride));
+    NS_TRY(dalloc(c, &c->ycoef, (size_t)d.jmax * ns::kCoefStride));
+    NS_TRY(dalloc(c, &c->sigx, (size_t)d.imax));
+    NS_TRY(dalloc(c, &c->sigy, (size_t)d.jmax));
+    NS_TRY(dalloc(c, &c->rhob, (size_t)d.jmax));
+    NS_TRY(dalloc(c, &c->psib, (size_t)d.jmax));
+    NS_TRY(dalloc(c, &c->stage_sin, 8));
+    NS_TRY(dalloc(c, &c->d_iter, 1));
+    NS_TRY(dalloc(c, &c->d_count, 1));
+    if (p->source_mode != NS_SRC_NONE) NS_TRY(dalloc(c, &c->src, P));
+
+    {
+        // zero everything so padding and never-written planes are defined
+        double *z[] = {c->U, c->U2, c->W, c->dudm, c->dudn, c->Ubase};
+        for (double *b : z) {
+            e = cudaMemsetAsync(b, 0, nk * P * sizeof(double), c->stream);
+            if (e != cudaSuccess) { rc = cuda_err(c, e, "cudaMemset"); goto fail; }
+        }
+        e = cudaMemsetAsync(c->aux, 0, (size_t)ns::AUX_COUNT * P * sizeof(double), c->stream);
+        if (e != cudaSuccess) { rc = cuda_err(c, e, "cudaMemset"); goto fail; }
+        e = cudaMemsetAsync(c->stage_sin, 0, 8 * sizeof(double), c->stream);
+        if (e != cudaSuccess) { rc = cuda_err(c, e, "cudaMemset"); goto fail; }
+        e = cudaMemsetAsync(c->d_iter, 0, sizeof(int), c->stream);
+        if (e != cudaSuccess) { rc = cuda_err(c, e, "cudaMemset"); goto fail; }
+    }
+
+    {
+        std::vector<double> tx, ty;
+        build_coef(tx, d.imax, p->dm, p->meshx, d.D, p->metric_mode);
+        build_coef(ty, d.jmax, p->dn, p->meshy, d.D, p->metric_mode);
+        e = cudaMemcpyAsync(c->xcoef, tx.data(), tx.size() * 8, cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(c->ycoef, ty.data(), ty.size() * 8, cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(c->sigx, p->sigmax, (size_t)d.imax * 8, cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(c->sigy, p->sigmay, (size_t)d.jmax * 8, cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(c->rhob, p->rhob, (size_t)d.jmax * 8, cudaMemcpyHostToDevice, c->stream);
+        std::vector<double> psib(d.jmax, 0.0);
+        if (p->psib) std::memcpy(psib.data(), p->psib, (size_t)d.jmax * 8);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(c->psib, psib.data(), (size_t)d.jmax * 8, cudaMemcpyHostToDevice, c->stream);
+        std::vector<double> field;
+        if (e == cudaSuccess && p->source_mode != NS_SRC_NONE) {
+            // spatial part of s_acou (rk.f90:188-189); the time factor is
+            // applied per stage on the device
+            field.assign((size_t)d.jmax * d.pitch, 0.0);
+            for (int j = 0; j < d.jmax; j++)
+                for (int i = 0; i < d.imax; i++) {
+                    double v;
+                    if (p->source_mode == NS_SRC_GAUSSIAN) {
+                        const double dx = p->m[i] - p->m_pt, dy = p->n[j] - p->n_pt;
+                        v = p->amplitude *
+                            std::exp(-(std::log(2.0) * (dx * dx + dy * dy) / (p->r0 * p->r0)));
+                    } else {
+                        v = p->src_field[(size_t)j * d.imax + i];
+                    }
+                    field[(size_t)j * d.pitch + i] = v;
+                }
+            e = cudaMemcpyAsync(c->src, field.data(), field.size() * 8, cudaMemcpyHostToDevice,
+                                c->stream);
+        }
+        if (e != cudaSuccess) { rc = cuda_err(c, e, "upload setup arrays"); goto fail; }
+        rc = upload_field(c, p->Ub, p->ub_layout, c->Ubase);
+        if (rc != NS_OK) goto fail;
+        // the setup vectors above must stay alive until the copies finish
+        e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) { rc = cuda_err(c, e, "setup"); goto fail; }
+    }
+
+    // constants
+    {
+        ns::Physics &ph = c->phys;
+        ph.gamma = p->gamma;
+        ph.dt = p->dt;
+        ph.inv_pe = 1.0 / kPe;
+        ph.alpha_cond = kAlphaCond;
+        if (c->visc) {
+            ph.inv_re = 1.0 / p->Re;
+            ph.inv_re_pr = 1.0 / p->Re / p->Pr;
+            ph.gm1_re = (p->gamma - 1.0) / p->Re;
+        } else {
+            ph.inv_re = ph.inv_re_pr = ph.gm1_re = 0.0;
+        }
+        ph.Tref = p->Tref;
+        ph.A_mi = p->A_mi; ph.B_mi = p->B_mi; ph.C_mi = p->C_mi; ph.D_mi = p->D_mi;
+        ph.A_k = p->A_k; ph.B_k = p->B_k; ph.C_k = p->C_k; ph.D_k = p->D_k;
+        if (c->visc) {
+            // GET_COEFFICIENTS, coefficients.f90:78-79
+            const double Tr = p->Tref;
+            const double k0 = std::exp(p->A_k * std::log(1.0 * Tr) + p->B_k / Tr + p->C_k / Tr / Tr + p->D_k);
+            const double mi0 = std::exp(p->A_mi * std::log(1.0 * Tr) + p->B_mi / Tr + p->C_mi / Tr / Tr + p->D_mi);
+            ph.mu0inv = 1.0 / mi0;
+            ph.k0inv = 1.0 / k0;
+        }
+        c->fx = make_filter(p->sigmaf, kDfbX);
+        c->fy = make_filter(p->sigmaf, kDfbY);
+        for (int k = 0; k < 6; k++) {
+            c->ct[k] = kCt[k];
+            c->alpha[k] = kAlpha[k];
+            c->beta[k] = kBeta[k];
+        }
+        c->warm = filter_warmup(p->sigmaf);
+        int nsm = 152;
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->dev);
+        const int target = nsm * 4 * 2 * 32;  // about two warps per SM sub-partition
+        c->fx_chunks = choose_chunks(d.jmax * d.nk, d.imax, c->warm, target);
+        c->fy_chunks = choose_chunks(d.imax * d.nk, d.jmax, c->warm, target);
+        c->launches_per_step = ns::count_step_launches(c);
+    }
+#undef NS_TRY
+    *out = c;
+    return NS_OK;
+fail:
+    free_all(c);
+    {
+        std::string msg = c->err;
+        delete c;
+        g_last_error = msg;
+    }
+    return rc;
+}
+
+void ns_destroy(ns_ctx *ctx)
+{
+    if (!ctx) return;
+    cudaSetDevice(ctx->dev);
+    cudaStreamSynchronize(ctx->stream);
+    free_all(ctx);
+    delete ctx;
+}
+
+int ns_set_state(ns_ctx *c, const double *U, int layout)
+{
+    if (!c || !U) return set_err(c, NS_ERR_PARAM, "ns_set_state: NULL argument");
+    NS_CUDA(c, cudaSetDevice(c->dev));
+    int rc = upload_field(c, U, layout, c->U);
+    if (rc != NS_OK) return rc;
+    NS_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->have_state = true;
+    return NS_OK;
+}
+
+int ns_get_state(ns_ctx *c, double *U, int layout)
+{
+    if (!c || !U) return set_err(c, NS_ERR_PARAM, "ns_get_state: NULL argument");
+    if (!c->have_state) return set_err(c, NS_ERR_STATE, "ns_get_state before ns_set_state");
+    NS_CUDA(c, cudaSetDevice(c->dev));
+    const ns::Dims &d = c->d;
+    const size_t row = (size_t)d.imax * sizeof(double);
+    if (layout == NS_LAYOUT_SOA) {
+        NS_CUDA(c, cudaMemcpy2DAsync(U, row, c->U, d.pitch * sizeof(double), row,
+                                     (size_t)d.jmax * d.nk, cudaMemcpyDeviceToHost, c->stream));
+    } else if (layout == NS_LAYOUT_FORTRAN) {
+        NS_CUDA(c, ns::launch_soa_to_aos(c->U, c->U2, d, c->stream));
+        NS_CUDA(c, cudaMemcpyAsync(U, c->U2, (size_t)d.nk * d.imax * d.jmax * sizeof(double),
+                                   cudaMemcpyDeviceToHost, c->stream));
+    } else {
+        return set_err(c, NS_ERR_PARAM, "layout=%d", layout);
+    }
+    NS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return NS_OK;
+}
+
+static int ensure_graph(ns_ctx *c)
+{
+    if (c->step_exec) return NS_OK;
+    cudaStream_t cs;
+    NS_CUDA(c, cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        cudaError_t le = ns::launch_step(c, cs);
+        e = cudaStreamEndCapture(cs, &g);
+        if (le != cudaSuccess) e = le;
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&c->step_exec, g, 0);
+    if (g) cudaGraphDestroy(g);
+    cudaStreamDestroy(cs);
+    if (e != cudaSuccess) {
+        c->step_exec = nullptr;
+        cudaGetLastError();
+        return cuda_err(c, e, "capture of the step graph");
+    }
+    return NS_OK;
+}
+
+int ns_step(ns_ctx *c, int iter0, int nsteps)
+{
+    if (!c) return set_err(nullptr, NS_ERR_PARAM, "ns_step: NULL context");
+    if (nsteps < 0) return set_err(c, NS_ERR_PARAM, "nsteps=%d", nsteps);
+    if (!c->have_state) return set_err(c, NS_ERR_STATE, "ns_step before ns_set_state");
+    if (nsteps == 0) return NS_OK;
+    NS_CUDA(c, cudaSetDevice(c->dev));
+    int rc = ensure_graph(c);
+    if (rc != NS_OK) return rc;
+    if (c->src) NS_CUDA(c, ns::launch_set_iter(c->d_iter, iter0, c->stream));
+    for (int s = 0; s < nsteps; s++) NS_CUDA(c, cudaGraphLaunch(c->step_exec, c->stream));
+    return NS_OK;
+}
+
+int ns_synchronize(ns_ctx *c)
+{
+    if (!c) return set_err(nullptr, NS_ERR_PARAM, "ns_synchronize: NULL context");
+    NS_CUDA(c, cudaSetDevice(c->dev));
+    NS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return NS_OK;
+}
+
+int ns_rk_euler(ns_ctx *c, double *U, double t, int iter, int nk)
+{
+    (void)t;
+    if (!c || !U) return set_err(c, NS_ERR_PARAM, "ns_rk_euler: NULL argument");
+    if (nk != c->d.nk) return set_err(c, NS_ERR_PARAM, "nk=%d, context has %d", nk, c->d.nk);
+    int rc = ns_set_state(c, U, NS_LAYOUT_FORTRAN);
+    if (rc == NS_OK) rc = ns_step(c, iter, 1);
+    if (rc == NS_OK) rc = ns_get_state(c, U, NS_LAYOUT_FORTRAN);
+    return rc;
+}
+
+int ns_get_probes(ns_ctx *c, int np, const int32_t *pi, const int32_t *pj, double *out)
+{
+    if (!c || np < 0 || (np > 0 && (!pi || !pj || !out)))
+        return set_err(c, NS_ERR_PARAM, "ns_get_probes: bad argument");
+    if (np == 0) return NS_OK;
+    if (!c->have_state) return set_err(c, NS_ERR_STATE, "ns_get_probes before ns_set_state");
+    std::vector<int32_t> idx(2 * (size_t)np);
+    for (int q = 0; q < np; q++) {
+        if (pi[q] < 1 || pi[q] > c->d.imax || pj[q] < 1 || pj[q] > c->d.jmax)
+            return set_err(c, NS_ERR_PARAM, "probe %d at (%d,%d) is outside the grid", q, pi[q], pj[q]);
+        idx[2 * q] = pi[q];
+        idx[2 * q + 1] = pj[q];
+    }
+    NS_CUDA(c, cudaSetDevice(c->dev));
+    if (np > c->probe_cap) {
+        if (c->probe_buf) cudaFree(c->probe_buf);
+        if (c->probe_idx) cudaFree(c->probe_idx);
+        c->probe_buf = nullptr;
+        c->probe_idx = nullptr;
+        c->probe_cap = 0;
+        int rc = dalloc(c, &c->probe_buf, (size_t)np * c->d.nk);
+        if (rc == NS_OK) rc = dalloc(c, &c->probe_idx, 2 * (size_t)np);
+        if (rc != NS_OK) return rc;
+        c->probe_cap = np;
+    }
+    NS_CUDA(c, cudaMemcpyAsync(c->probe_idx, idx.data(), idx.size() * sizeof(int32_t),
+                               cudaMemcpyHostToDevice, c->stream));
+    NS_CUDA(c, ns::launch_probes(c->U, c->d, np, c->probe_idx, c->probe_buf, c->stream));
+    NS_CUDA(c, cudaMemcpyAsync(out, c->probe_buf, (size_t)np * c->d.nk * sizeof(double),
+                               cudaMemcpyDeviceToHost, c->stream));
+    NS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return NS_OK;
+}
+
+int ns_check_finite(ns_ctx *c, int64_t *nonfinite)
+{
+    if (!c) return set_err(nullptr, NS_ERR_PARAM, "ns_check_finite: NULL context");
+    if (!c->have_state) return set_err(c, NS_ERR_STATE, "ns_check_finite before ns_set_state");
+    NS_CUDA(c, cudaSetDevice(c->dev));
+    unsigned long long h = 0;
+    NS_CUDA(c, cudaMemsetAsync(c->d_count, 0, sizeof(unsigned long long), c->stream));
+    NS_CUDA(c, ns::launch_count_nonfinite(c->U, c->d, c->d_count, c->stream));
+    NS_CUDA(c, cudaMemcpyAsync(&h, c->d_count, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+    NS_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (nonfinite) *nonfinite = (int64_t)h;
+    if (h) return set_err(c, NS_ERR_NONFINITE, "%llu non-finite values in the state", h);
+    return NS_OK;
+}
+
+int ns_set_stream(ns_ctx *c, void *stream)
+{
+    if (!c) return set_err(nullptr, NS_ERR_PARAM, "ns_set_stream: NULL context");
+    c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+    return NS_OK;
+}
+
+int ns_get_stream(ns_ctx *c, void **stream)
+{
+    if (!c || !stream) return set_err(c, NS_ERR_PARAM, "ns_get_stream: NULL argument");
+    *stream = (void *)c->stream;
+    return NS_OK;
+}
+
+int ns_state_device(ns_ctx *c, void **dptr, int64_t *pitch)
+{
+    if (!c || !dptr || !pitch) return set_err(c, NS_ERR_PARAM, "ns_state_device: NULL argument");
+    *dptr = (void *)c->U;
+    *pitch = c->d.pitch;
+    return NS_OK;
+}
+
+int ns_step_launches(ns_ctx *c, int *launches)
+{
+    if (!c || !launches) return set_err(c, NS_ERR_PARAM, "ns_step_launches: NULL argument");
+    *launches = c->launches_per_step;
+    return NS_OK;
+}
+
+int ns_filter_warmup(ns_ctx *c, int *warmup)
+{
+    if (!c || !warmup) return set_err(c, NS_ERR_PARAM, "ns_filter_warmup: NULL argument");
+    *warmup = c->warm;
+    return NS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,112 @@
+// ns_internal.cuh -- shared definitions of the GB300 time-step library.
+//
+// Device layout (all FP64 unless noted): every 2-D field is a plane of
+// jmax rows of `pitch` doubles (pitch = imax rounded up to 32, so each row
+// starts on a 256-byte boundary); variable k of a multi-variable field is
+// plane k.  Index (i,j) (0-based; the reference's (i+1,j+1)) is at
+// j*pitch + i.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+
+#include "../../include/ns_gb300.h"
+
+namespace ns {
+
+constexpr int kMaxNk = 5;
+
+// Planes of the auxiliary field `aux`.
+enum AuxPlane {
+    AUX_T = 0,     // T = gamma*p/rho                      (rhs.f90:20)
+    AUX_RINV = 1,  // 1/rho
+    AUX_TAU1 = 2,  // tau_xx                               (eqeuler.f90:37)
+    AUX_TAU2 = 3,  // tau_xy                               (eqeuler.f90:38)
+    AUX_TAU3 = 4,  // tau_yy                               (eqeuler.f90:39)
+    AUX_KTX = 5,   // k * dT/dx                            (derivs.f90:48-56)
+    AUX_KTY = 6,   // k * dT/dy
+    AUX_PSID = 7,  // rho*alpha_cond*(dpsi/dx+dpsi/dy)      (derivs.f90:37)
+    AUX_COUNT = 8
+};
+
+struct Dims {
+    int imax, jmax, pitch, nk, D;
+    long long plane;  // pitch * jmax
+};
+
+// Per-line derivative coefficients: 8 doubles per line position q.  For an
+// interior position entries 4..6 hold a_s*metric/h (s = 1..3) and the
+// derivative is sum_s c_s*(f[q+s]-f[q-s]); for the three closure positions
+// at each end, entries 0..6 hold the 7 one-sided coefficients for offsets
+// o0..o0+6 (o0 = -q at the left end, n-7-q at the right end).
+constexpr int kCoefStride = 8;
+
+// Filter coefficients pre-multiplied by the filter strength.
+struct FilterCoef {
+    double c0;       // 1 - sigmaf*df(0)
+    double m[7];     // m[s] = -sigmaf*df(s), s = 1..6 (m[0] unused)
+    double b0;       // 1 - sigmaf*dfb(0)
+    double bm1;      // -sigmaf*dfb(-1)
+    double b[6];     // b[s] = -sigmaf*dfb(s), s = 1..5 (b[0] unused)
+};
+
+struct Physics {
+    double gamma, inv_re, inv_re_pr, gm1_re, dt, inv_pe, alpha_cond;
+    double Tref, mu0inv, k0inv;
+    double A_mi, B_mi, C_mi, D_mi, A_k, B_k, C_k, D_k;
+};
+
+struct StageCoef {
+    double alpha, beta;
+    int stage;
+};
+
+}  // namespace ns
+
+struct ns_ctx {
+    ns_params p;
+    ns::Dims d;
+    int dev = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    // device buffers
+    double *U = nullptr, *U2 = nullptr, *W = nullptr;
+    double *dudm = nullptr, *dudn = nullptr, *aux = nullptr;
+    double *Ubase = nullptr, *src = nullptr;
+    double *xcoef = nullptr, *ycoef = nullptr;
+    double *sigx = nullptr, *sigy = nullptr, *rhob = nullptr, *psib = nullptr;
+    double *stage_sin = nullptr;
+    int *d_iter = nullptr;
+    unsigned long long *d_count = nullptr;
+    double *probe_buf = nullptr;
+    int probe_cap = 0;
+    int32_t *probe_idx = nullptr;
+    // host-side constants
+    ns::Physics phys;
+    ns::FilterCoef fx, fy;
+    double ct[6], alpha[6], beta[6];
+    int warm = 0;       // filter warm-up length (-1: serial sweeps)
+    int fx_chunks = 1, fy_chunks = 1;
+    bool visc = false;
+    bool have_state = false;
+    // captured one-step graph
+    cudaGraphExec_t step_exec = nullptr;
+    cudaStream_t graph_stream = nullptr;
+    int launches_per_step = 0;
+    std::string err;
+};
+
+// Kernel launchers (ns_kernels.cu).  All enqueue on `s` and return the
+// launch status.
+namespace ns {
+cudaError_t launch_step(ns_ctx *c, cudaStream_t s);
+cudaError_t launch_set_iter(int *d_iter, int iter, cudaStream_t s);
+cudaError_t launch_aos_to_soa(const double *in, double *out, const Dims &d, cudaStream_t s);
+cudaError_t launch_soa_to_aos(const double *in, double *out, const Dims &d, cudaStream_t s);
+cudaError_t launch_probes(const double *U, const Dims &d, int np, const int32_t *idx,
+                          double *out, cudaStream_t s);
+cudaError_t launch_count_nonfinite(const double *U, const Dims &d, unsigned long long *count,
+                                   cudaStream_t s);
+int count_step_launches(const ns_ctx *c);
+}  // namespace ns

@@ -1,0 +1,607 @@
+// ns_kernels.cu -- FP64 stage kernels of the LDDRK step (rk.f90:12-75).
+//
+// On GB300 the FP64 pipe (about 1.2 TFLOP/s, 1.9 DFMA/clk/SM) binds long
+// before HBM does, so the stage is split into kernels that never recompute
+// an FP64 quantity: every intermediate the reference keeps in module arrays
+// (TEMP, dUdm/dUdn, TAU, k*dT, psiDiff) is written once to HBM and read
+// back by the next kernel.  Per stage:
+//
+//   k_prim    (NS only)  T = gamma*p/rho, 1/rho              rhs.f90:20
+//   k_first              dU/dx, dU/dy (DRP + closures + metric), mu(T),
+//                        k(T), k*dT/dx, k*dT/dy, tau, psiDiff
+//                        diff.f90:6-151,276-350; derivs.f90:9-56;
+//                        coefficients.f90:27-59; eqeuler.f90:28-47
+//   k_update             second derivatives, EULERNONLINEAR, rk_steep,
+//                        bufferxy                  eqeuler.f90:53-99;
+//                                                  rk.f90:77-169
+//   k_filter<x>          lddfilterx as chunked recurrences  filtering.f90:9-96
+//   k_filter<y>          lddfiltery                         filtering.f90:98-190
+//   k_bc                 ccpml                              cc.f90:6-68
+#include "ns_internal.cuh"
+
+namespace ns {
+
+// ---------------------------------------------------------------------------
+// DRP first derivative along a line (diff.f90:40-238 with the metric of
+// diff.f90:276-350 folded into the coefficients).
+// f points at position q of a line of length n and stride st; c = the 8
+// coefficients of position q.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double dline(const double *__restrict__ f, long long st, int q,
+                                        int n, const double *__restrict__ c)
+{
+    if (q >= 3 && q < n - 3) {
+        const double c1 = c[4], c2 = c[5], c3 = c[6];
+        double r = c1 * (f[st] - f[-st]);
+        r = fma(c2, f[2 * st] - f[-2 * st], r);
+        r = fma(c3, f[3 * st] - f[-3 * st], r);
+        return r;
+    }
+    const int o0 = (q < 3) ? -q : (n - 7 - q);
+    const double *g = f + (long long)o0 * st;
+    double r = c[0] * g[0];
+#pragma unroll
+    for (int z = 1; z < 7; z++) r = fma(c[z], g[(long long)z * st], r);
+    return r;
+}
+
+// ---------------------------------------------------------------------------
+// k_prim: T and 1/rho (rhs.f90:20), pointwise.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_prim(Dims d, const double *__restrict__ U,
+                                              double *__restrict__ aux, double gamma)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= d.imax || j >= d.jmax) return;
+    const long long idx = (long long)j * d.pitch + i;
+    const double rho = U[idx];
+    const double p = U[3 * d.plane + idx];
+    const double ri = 1.0 / rho;
+    aux[AUX_RINV * d.plane + idx] = ri;
+    aux[AUX_T * d.plane + idx] = (gamma * p) * ri;
+}
+
+// ---------------------------------------------------------------------------
+// k_first: first derivatives and everything pointwise built from them.
+// ---------------------------------------------------------------------------
+template <bool VISC, int NK>
+__global__ void __launch_bounds__(256)
+    k_first(Dims d, const double *__restrict__ U, double *__restrict__ dudm,
+            double *__restrict__ dudn, double *__restrict__ aux,
+            const double *__restrict__ xcoef, const double *__restrict__ ycoef, Physics ph)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= d.imax || j >= d.jmax) return;
+    const long long idx = (long long)j * d.pitch + i;
+    const long long P = d.plane, st = d.pitch;
+    const double *cx = xcoef + kCoefStride * i;
+    const double *cy = ycoef + kCoefStride * j;
+    double gx[NK], gy[NK];
+#pragma unroll
+    for (int k = 0; k < NK; k++) {
+        const double *f = U + k * P + idx;
+        gx[k] = dline(f, 1, i, d.imax, cx);
+        gy[k] = dline(f, st, j, d.jmax, cy);
+        dudm[k * P + idx] = gx[k];
+        dudn[k * P + idx] = gy[k];
+    }
+    if (VISC) {
+        // dT/dx, dT/dy (derivs.f90:25-26), mu(T), k(T) (coefficients.f90:27-59)
+        const double *fT = aux + AUX_T * P + idx;
+        const double T = fT[0];
+        const double Tx = dline(fT, 1, i, d.imax, cx);
+        const double Ty = dline(fT, st, j, d.jmax, cy);
+        const double x = ph.Tref * T;
+        const double L = log(x);
+        const double y = 1.0 / x;
+        const double amu = fma(ph.A_mi, L, fma(fma(ph.C_mi, y, ph.B_mi), y, ph.D_mi));
+        const double ak = fma(ph.A_k, L, fma(fma(ph.C_k, y, ph.B_k), y, ph.D_k));
+        const double mu = ph.mu0inv * exp(amu);
+        const double kc = ph.k0inv * exp(ak);
+        aux[AUX_KTX * P + idx] = Tx * kc;  // kdT (derivs.f90:48-56)
+        aux[AUX_KTY * P + idx] = Ty * kc;
+        // TAU_IJ (eqeuler.f90:37-39)
+        const double div = gx[1] + gy[2];
+        const double m23 = (2.0 / 3.0) * mu;
+        const double mu2 = 2.0 * mu;
+        aux[AUX_TAU1 * P + idx] = fma(mu2, gx[1], -(m23 * div));
+        aux[AUX_TAU2 * P + idx] = mu * (gy[1] + gx[2]);
+        aux[AUX_TAU3 * P + idx] = fma(mu2, gy[2], -(m23 * div));
+    }
+    if (NK >= 5) {
+        const double rho = U[idx];
+        aux[AUX_PSID * P + idx] = (rho * ph.alpha_cond) * (gx[NK - 1] + gy[NK - 1]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// k_update: second-level derivatives, EULERNONLINEAR (eqeuler.f90:53-99),
+// rk_steep on the interior (rk.f90:153-169) and bufferxy on the bands
+// (rk.f90:77-151), all points of the grid.
+// ---------------------------------------------------------------------------
+template <bool VISC, int NK, bool FIRST, bool SRC>
+__global__ void __launch_bounds__(256)
+    k_update(Dims d, double *__restrict__ U, double *__restrict__ W,
+             const double *__restrict__ dudm, const double *__restrict__ dudn,
+             const double *__restrict__ aux, const double *__restrict__ xcoef,
+             const double *__restrict__ ycoef, const double *__restrict__ Ubase,
+             const double *__restrict__ sigx, const double *__restrict__ sigy,
+             const double *__restrict__ src, const double *__restrict__ stage_sin, Physics ph,
+             StageCoef sc)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= d.imax || j >= d.jmax) return;
+    const long long idx = (long long)j * d.pitch + i;
+    const long long P = d.plane, st = d.pitch;
+    double u[NK];
+#pragma unroll
+    for (int k = 0; k < NK; k++) u[k] = U[k * P + idx];
+
+    const bool interior = (i > 0) && (i < d.imax - 1) && (j > 0) && (j < d.jmax - 1);
+    if (interior) {
+        double gx[NK], gy[NK];
+#pragma unroll
+        for (int k = 0; k < NK; k++) {
+            gx[k] = dudm[k * P + idx];
+            gy[k] = dudn[k * P + idx];
+        }
+        const double rho = u[0], uu = u[1], vv = u[2], pp = u[3];
+        const double ri = VISC ? aux[AUX_RINV * P + idx] : 1.0 / rho;
+        double r[NK];
+        // DUDT(1), eqeuler.f90:63
+        double t = uu * gx[0];
+        t = fma(rho, gx[1], t);
+        t = fma(vv, gy[0], t);
+        t = fma(rho, gy[2], t);
+        r[0] = -t;
+        // DUDT(2), :68
+        double a2 = uu * gx[1];
+        a2 = fma(ri, gx[3], a2);
+        a2 = fma(vv, gy[1], a2);
+        // DUDT(3), :74
+        double a3 = uu * gx[2];
+        a3 = fma(vv, gy[2], a3);
+        a3 = fma(ri, gy[3], a3);
+        // DUDT(4), :80-92
+        const double gp = ph.gamma * pp;
+        double a4 = gp * gx[1];
+        a4 = fma(uu, gx[3], a4);
+        a4 = fma(gp, gy[2], a4);
+        a4 = fma(vv, gy[3], a4);
+        if (SRC) {
+            const double s = stage_sin[sc.stage] * src[idx];
+            a4 = a4 - s;
+        }
+        const double *cx = xcoef + kCoefStride * i;
+        const double *cy = ycoef + kCoefStride * j;
+        if (VISC) {
+            const double *t1 = aux + AUX_TAU1 * P + idx;
+            const double *t2 = aux + AUX_TAU2 * P + idx;
+            const double *t3 = aux + AUX_TAU3 * P + idx;
+            const double dt1x = dline(t1, 1, i, d.imax, cx);
+            const double dt2x = dline(t2, 1, i, d.imax, cx);
+            const double dt2y = dline(t2, st, j, d.jmax, cy);
+            const double dt3y = dline(t3, st, j, d.jmax, cy);
+            const double d2T = dline(aux + AUX_KTX * P + idx, 1, i, d.imax, cx) +
+                               dline(aux + AUX_KTY * P + idx, st, j, d.jmax, cy);
+            const double rv = ph.inv_re * ri;
+            a2 = fma(-rv, dt1x + dt2y, a2);
+            a3 = fma(-rv, dt2x + dt3y, a3);
+            const double tau1 = t1[0], tau2 = t2[0], tau3 = t3[0];
+            double phi = gx[1] * tau1;
+            phi = fma(gx[2], tau2, phi);
+            phi = fma(gy[1], tau2, phi);
+            phi = fma(gy[2], tau3, phi);
+            a4 = fma(-ph.gm1_re, phi, a4);
+            a4 = fma(-ph.inv_re_pr, d2T, a4);
+        }
+        r[1] = -a2;
+        r[2] = -a3;
+        r[3] = -a4;
+        if (NK >= 5) {
+            // DUDT(5), :94-95
+            const double *pd = aux + AUX_PSID * P + idx;
+            const double d2p = dline(pd, 1, i, d.imax, cx) + dline(pd, st, j, d.jmax, cy);
+            double a5 = uu * gx[NK - 1];
+            a5 = fma(vv, gy[NK - 1], a5);
+            a5 = fma(-(ph.inv_pe * ri), d2p, a5);
+            r[NK - 1] = -a5;
+        }
+        // rk_steep (rk.f90:163-164)
+#pragma unroll
+        for (int k = 0; k < NK; k++) {
+            double w;
+            if (FIRST)
+                w = ph.dt * r[k];
+            else
+                w = fma(sc.alpha, W[k * P + idx], ph.dt * r[k]);
+            W[k * P + idx] = w;
+            u[k] = fma(sc.beta, w, u[k]);
+        }
+    }
+    // bufferxy: buffery then bufferx at each point (rk.f90:86-105, :123, :145)
+    const bool by = (j < d.D) || (j >= d.jmax - d.D);
+    const bool bx = (i < d.D) || (i >= d.imax - d.D);
+    if (by || bx) {
+        double ub[NK];
+#pragma unroll
+        for (int k = 0; k < NK; k++) ub[k] = Ubase[k * P + idx];
+        if (by) {
+            const double s = sigy[j];
+#pragma unroll
+            for (int k = 0; k < NK; k++) u[k] = fma(s, u[k] - ub[k], ub[k]);
+        }
+        if (bx) {
+            const double s = sigx[i];
+#pragma unroll
+            for (int k = 0; k < NK; k++) u[k] = fma(s, u[k] - ub[k], ub[k]);
+        }
+    }
+    if (interior || by || bx) {
+#pragma unroll
+        for (int k = 0; k < NK; k++) U[k * P + idx] = u[k];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// k_filter: the in-place selective filter sweeps of filtering.f90 along x
+// (ALONG_Y = false) or y, out of place (src -> dst).
+//
+// Each line (k,j) or (k,i) is one recurrence: pass 1 ascends positions
+// 1..6 with the 7-point boundary filter, pass 2 ascends 6..n-7 with the
+// 13-point filter, pass 3 descends n-2..n-7 with the mirrored boundary
+// filter; each point's stencil reads the already-filtered points before it
+// (0-based positions; the reference's i = q+1).  A line is split into
+// chunks over pass 2.  A chunk whose start lies more than `warm` points
+// past position 6 starts the recurrence `warm` points early from unfiltered
+// history; the error of that history decays by the spectral radius of the
+// recurrence at every point, and `warm` is chosen on the host so that it
+// falls below 2^-60 of the data before the chunk's first output.
+// ---------------------------------------------------------------------------
+template <bool ALONG_Y>
+__global__ void __launch_bounds__(128)
+    k_filter(Dims d, const double *__restrict__ src, double *__restrict__ dst, int chunks,
+             int warm, FilterCoef fc)
+{
+    const int nlines = ALONG_Y ? d.imax : d.jmax;
+    const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long total = (long long)nlines * d.nk * chunks;
+    if (gid >= total) return;
+    const int line = (int)(gid % nlines);
+    const int rest = (int)(gid / nlines);
+    const int k = rest % d.nk;
+    const int c = rest / d.nk;
+    const int n = ALONG_Y ? d.jmax : d.imax;
+    const long long st = ALONG_Y ? d.pitch : 1;
+    const long long base = (long long)k * d.plane + (ALONG_Y ? line : (long long)line * d.pitch);
+    const double *__restrict__ s = src + base;
+    double *__restrict__ o = dst + base;
+
+    const int len2 = n - 12;  // pass-2 positions 6 .. n-7
+    const int a = 6 + (int)(((long long)c * len2) / chunks);
+    const int b = 6 + (int)(((long long)(c + 1) * len2) / chunks);
+    const bool last = (c == chunks - 1);
+
+    double w[13];
+    int q;
+    if (c == 0 || warm < 0 || a - warm <= 6) {
+        // exact start: pass 1 (filtering.f90:39-49 / :128-140)
+#pragma unroll
+        for (int t = 0; t < 13; t++) w[t] = s[t * st];
+#pragma unroll
+        for (int p = 1; p <= 6; p++) {
+            double v = fc.b0 * w[p];
+#pragma unroll
+            for (int z = 1; z <= 5; z++) v = fma(fc.b[z], w[p + z], v);
+            v = fma(fc.bm1, w[p - 1], v);
+            w[p] = v;
+        }
+        if (c == 0) {
+#pragma unroll
+            for (int p = 0; p < 6; p++) o[p * st] = w[p];
+        }
+        q = 6;
+    } else {
+        q = a - warm;
+#pragma unroll
+        for (int t = 0; t < 13; t++) w[t] = s[(long long)(q - 6 + t) * st];
+    }
+    // pass 2 (filtering.f90:69-79 / :161-171)
+    for (; q < b; q++) {
+        double v = fc.c0 * w[6];
+        v = fma(fc.m[6], w[12] + w[0], v);
+        v = fma(fc.m[5], w[11] + w[1], v);
+        v = fma(fc.m[4], w[10] + w[2], v);
+        v = fma(fc.m[3], w[9] + w[3], v);
+        v = fma(fc.m[2], w[8] + w[4], v);
+        v = fma(fc.m[1], w[7], v);
+        v = fma(fc.m[1], w[5], v);
+        if (q >= a) o[(long long)q * st] = v;
+#pragma unroll
+        for (int t = 0; t < 5; t++) w[t] = w[t + 1];
+        w[5] = v;
+#pragma unroll
+        for (int t = 6; t < 12; t++) w[t] = w[t + 1];
+        w[12] = (q + 7 < n) ? s[(long long)(q + 7) * st] : 0.0;
+    }
+    if (last) {
+        // pass 3 (filtering.f90:84-94 / :176-188): w[0..11] = positions n-12..n-1
+#pragma unroll
+        for (int x = 10; x >= 5; x--) {
+            double v = fc.b0 * w[x];
+#pragma unroll
+            for (int z = 1; z <= 5; z++) v = fma(fc.b[z], w[x - z], v);
+            v = fma(fc.bm1, w[x + 1], v);
+            w[x] = v;
+        }
+#pragma unroll
+        for (int x = 5; x < 12; x++) o[(long long)(n - 12 + x) * st] = w[x];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// k_bc: ccpml (cc.f90:6-68).  Thread t < jmax sets row t of the left and
+// right columns (cc.f90:23-36, corners excepted); thread t < imax sets
+// column t of the top and bottom rows (cc.f90:39-59), recomputing the
+// column values it extrapolates from at i = 1 and i = imax, so no thread
+// reads a location another thread writes.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void bc_column_values(const double *__restrict__ U, const Dims &d,
+                                                 int i, int j, const double *__restrict__ rhob,
+                                                 const double *__restrict__ psib, double gamma,
+                                                 double *v)
+{
+    const long long P = d.plane;
+    const long long r = (long long)j * d.pitch;
+    if (i == 0) {
+        v[0] = rhob[j];
+        v[1] = 2.0 * U[1 * P + r + 1] - U[1 * P + r + 2];
+        v[2] = 0.0;
+        v[3] = 1.0 / gamma;
+        if (d.nk >= 5) v[4] = psib[j];
+    } else {
+        const int a = d.imax - 2, b = d.imax - 3;
+        for (int k = 0; k < d.nk; k++) v[k] = 2.0 * U[k * P + r + a] - U[k * P + r + b];
+        v[3] = 1.0 / gamma;
+    }
+}
+
+__global__ void k_bc(Dims d, double *__restrict__ U, const double *__restrict__ rhob,
+                     const double *__restrict__ psib, double gamma)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const long long P = d.plane;
+    double v[kMaxNk];
+    if (t > 0 && t < d.jmax - 1) {
+        const long long r = (long long)t * d.pitch;
+        bc_column_values(U, d, 0, t, rhob, psib, gamma, v);
+        for (int k = 0; k < d.nk; k++) U[k * P + r] = v[k];
+        bc_column_values(U, d, d.imax - 1, t, rhob, psib, gamma, v);
+        for (int k = 0; k < d.nk; k++) U[k * P + r + d.imax - 1] = v[k];
+    }
+    if (t < d.imax) {
+        const int jt = d.jmax - 1;
+        double a[kMaxNk], b[kMaxNk];
+        // top (cc.f90:39-43)
+        if (t == 0 || t == d.imax - 1) {
+            bc_column_values(U, d, t, jt - 1, rhob, psib, gamma, a);
+            bc_column_values(U, d, t, jt - 2, rhob, psib, gamma, b);
+        } else {
+            for (int k = 0; k < d.nk; k++) {
+                a[k] = U[k * P + (long long)(jt - 1) * d.pitch + t];
+                b[k] = U[k * P + (long long)(jt - 2) * d.pitch + t];
+            }
+        }
+        for (int k = 0; k < 3; k++) U[k * P + (long long)jt * d.pitch + t] = 2.0 * a[k] - b[k];
+        U[3 * P + (long long)jt * d.pitch + t] = 1.0 / gamma;
+        if (d.nk >= 5) U[4 * P + (long long)jt * d.pitch + t] = 1.0;
+        // bottom (cc.f90:55-59)
+        if (t == 0 || t == d.imax - 1) {
+            bc_column_values(U, d, t, 1, rhob, psib, gamma, a);
+            bc_column_values(U, d, t, 2, rhob, psib, gamma, b);
+        } else {
+            for (int k = 0; k < d.nk; k++) {
+                a[k] = U[k * P + (long long)1 * d.pitch + t];
+                b[k] = U[k * P + (long long)2 * d.pitch + t];
+            }
+        }
+        for (int k = 0; k < 3; k++) U[k * P + t] = 2.0 * a[k] - b[k];
+        U[3 * P + t] = 1.0 / gamma;
+        if (d.nk >= 5) U[4 * P + t] = 0.0;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Per-step source phase: stage_sin[k] = sin(wf*((iter+c_k)*dt)) for the six
+// stages (rk.f90:188), then the device step counter advances.
+// ---------------------------------------------------------------------------
+struct SinArgs {
+    double wf, dt, ct[6];
+};
+
+__global__ void k_stage_sin(int *d_iter, double *stage_sin, SinArgs a)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int iter = *d_iter;
+    for (int k = 0; k < 6; k++) stage_sin[k] = sin(a.wf * (((double)iter + a.ct[k]) * a.dt));
+    *d_iter = iter + 1;
+}
+
+__global__ void k_set_iter(int *d_iter, int iter) { *d_iter = iter; }
+
+// ---------------------------------------------------------------------------
+// Layout conversion, probes, finite check
+// ---------------------------------------------------------------------------
+__global__ void k_aos_to_soa(const double *__restrict__ in, double *__restrict__ out, Dims d)
+{
+    const long long n = (long long)d.nk * d.imax * d.jmax;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(e % d.nk);
+        const long long pt = e / d.nk;
+        const int i = (int)(pt % d.imax);
+        const int j = (int)(pt / d.imax);
+        out[k * d.plane + (long long)j * d.pitch + i] = in[e];
+    }
+}
+
+__global__ void k_soa_to_aos(const double *__restrict__ in, double *__restrict__ out, Dims d)
+{
+    const long long n = (long long)d.nk * d.imax * d.jmax;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(e % d.nk);
+        const long long pt = e / d.nk;
+        const int i = (int)(pt % d.imax);
+        const int j = (int)(pt / d.imax);
+        out[e] = in[k * d.plane + (long long)j * d.pitch + i];
+    }
+}
+
+__global__ void k_probes(const double *__restrict__ U, Dims d, int np,
+                         const int32_t *__restrict__ idx, double *__restrict__ out)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= np * d.nk) return;
+    const int p = t / d.nk, k = t % d.nk;
+    const int i = idx[2 * p] - 1, j = idx[2 * p + 1] - 1;
+    out[t] = U[k * d.plane + (long long)j * d.pitch + i];
+}
+
+__global__ void k_count_nonfinite(const double *__restrict__ U, Dims d,
+                                  unsigned long long *count)
+{
+    unsigned long long local = 0;
+    const long long n = (long long)d.nk * d.jmax * d.imax;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(e % d.imax);
+        const long long r = e / d.imax;  // k*jmax + j
+        const double v = U[r * d.pitch + i];
+        if (!isfinite(v)) local++;
+    }
+    for (int o = 16; o > 0; o >>= 1) local += __shfl_down_sync(0xffffffffu, local, o);
+    if ((threadIdx.x & 31) == 0 && local) atomicAdd(count, local);
+}
+
+// ---------------------------------------------------------------------------
+// Host launchers
+// ---------------------------------------------------------------------------
+static inline dim3 tile_grid(const Dims &d, dim3 blk)
+{
+    return dim3((d.imax + blk.x - 1) / blk.x, (d.jmax + blk.y - 1) / blk.y);
+}
+
+template <bool VISC, int NK>
+static cudaError_t launch_stage_t(ns_ctx *c, int stage, cudaStream_t s)
+{
+    const Dims &d = c->d;
+    const dim3 blk(32, 8);
+    const dim3 grd = tile_grid(d, blk);
+    if (VISC) k_prim<<<grd, blk, 0, s>>>(d, c->U, c->aux, c->phys.gamma);
+    k_first<VISC, NK><<<grd, blk, 0, s>>>(d, c->U, c->dudm, c->dudn, c->aux, c->xcoef, c->ycoef,
+                                          c->phys);
+    StageCoef sc{c->alpha[stage], c->beta[stage], stage};
+    const bool src = c->src != nullptr;
+#define NS_UPD(FIRST, SRC)                                                                    \
+    k_update<VISC, NK, FIRST, SRC><<<grd, blk, 0, s>>>(d, c->U, c->W, c->dudm, c->dudn,       \
+                                                       c->aux, c->xcoef, c->ycoef, c->Ubase,  \
+                                                       c->sigx, c->sigy, c->src, c->stage_sin, \
+                                                       c->phys, sc)
+    if (stage == 0) {
+        if (src) NS_UPD(true, true); else NS_UPD(true, false);
+    } else {
+        if (src) NS_UPD(false, true); else NS_UPD(false, false);
+    }
+#undef NS_UPD
+    {
+        const long long tx = (long long)d.jmax * d.nk * c->fx_chunks;
+        k_filter<false><<<(unsigned)((tx + 127) / 128), 128, 0, s>>>(d, c->U, c->U2,
+                                                                     c->fx_chunks, c->warm, c->fx);
+        const long long ty = (long long)d.imax * d.nk * c->fy_chunks;
+        k_filter<true><<<(unsigned)((ty + 127) / 128), 128, 0, s>>>(d, c->U2, c->U, c->fy_chunks,
+                                                                    c->warm, c->fy);
+    }
+    {
+        const int nt = d.imax > d.jmax ? d.imax : d.jmax;
+        k_bc<<<(nt + 127) / 128, 128, 0, s>>>(d, c->U, c->rhob, c->psib, c->phys.gamma);
+    }
+    return cudaGetLastError();
+}
+
+static cudaError_t launch_stage(ns_ctx *c, int stage, cudaStream_t s)
+{
+    if (c->visc)
+        return c->d.nk == 5 ? launch_stage_t<true, 5>(c, stage, s)
+                            : launch_stage_t<true, 4>(c, stage, s);
+    return c->d.nk == 5 ? launch_stage_t<false, 5>(c, stage, s)
+                        : launch_stage_t<false, 4>(c, stage, s);
+}
+
+cudaError_t launch_step(ns_ctx *c, cudaStream_t s)
+{
+    if (c->src) {
+        SinArgs a;
+        a.wf = c->p.wf;
+        a.dt = c->p.dt;
+        for (int k = 0; k < 6; k++) a.ct[k] = c->ct[k];
+        k_stage_sin<<<1, 32, 0, s>>>(c->d_iter, c->stage_sin, a);
+    }
+    for (int stage = 0; stage < 6; stage++) {
+        cudaError_t e = launch_stage(c, stage, s);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaGetLastError();
+}
+
+int count_step_launches(const ns_ctx *c)
+{
+    const int per_stage = (c->visc ? 1 : 0) + 1 + 1 + 2 + 1;
+    return 6 * per_stage + (c->src ? 1 : 0);
+}
+
+cudaError_t launch_set_iter(int *d_iter, int iter, cudaStream_t s)
+{
+    k_set_iter<<<1, 1, 0, s>>>(d_iter, iter);
+    return cudaGetLastError();
+}
+
+static inline unsigned grid_for(long long n)
+{
+    long long b = (n + 255) / 256;
+    if (b > 152 * 16) b = 152 * 16;
+    if (b < 1) b = 1;
+    return (unsigned)b;
+}
+
+cudaError_t launch_aos_to_soa(const double *in, double *out, const Dims &d, cudaStream_t s)
+{
+    k_aos_to_soa<<<grid_for((long long)d.nk * d.imax * d.jmax), 256, 0, s>>>(in, out, d);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_soa_to_aos(const double *in, double *out, const Dims &d, cudaStream_t s)
+{
+    k_soa_to_aos<<<grid_for((long long)d.nk * d.imax * d.jmax), 256, 0, s>>>(in, out, d);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_probes(const double *U, const Dims &d, int np, const int32_t *idx,
+                          double *out, cudaStream_t s)
+{
+    const int n = np * d.nk;
+    k_probes<<<(n + 127) / 128, 128, 0, s>>>(U, d, np, idx, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_count_nonfinite(const double *U, const Dims &d, unsigned long long *count,
+                                   cudaStream_t s)
+{
+    k_count_nonfinite<<<grid_for((long long)d.nk * d.imax * d.jmax), 256, 0, s>>>(U, d, count);
+    return cudaGetLastError();
+}
+
+}  // namespace ns
