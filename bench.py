@@ -1,0 +1,367 @@
+#!/usr/bin/env python3
+"""Throughput of the LDDRK time step (rk.f90:12-75) on GB300.
+
+Workload: the 4096x2048 Navier-Stokes case on the y-stretched grid (FP64,
+rho,u,v,p), one "step" = one call of rk_euler over the whole grid (six
+stages: RHS, update, buffer, both filters, boundary conditions).  Metric:
+Mpt-steps/s = imax*jmax*steps / s / 1e6.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun each rank advances its own replica on its own GPU (the path
+has no exchange step: replicas only); the line reports the whole-job rate
+over the slowest rank.  `--impl reference` times the CPU oracle (the C
+restatement of the Fortran reference, which cannot be compiled here) on the
+host cores for the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Mpt-steps/s, FP64 vs split-precision at stated p' error; adjoint/fwd cost"
+UNIT = "Mpt-steps/s"
+
+# Algorithmic HBM bytes per grid point of one launch of each kernel class
+# (every input read once, every output written once; nk = 4, Navier-Stokes):
+#   k_prim:     rho, p in; T, 1/rho out                          4*8
+#   k_first:    U(4) + T in; dU/dx(4), dU/dy(4), tau(3), k*grad T(2) out
+#   k_update:   U, w, dU/dx, dU/dy, tau, k*grad T, 1/rho in; U, w out
+#   k_filter_*: U in, U out
+BYTES_PER_POINT = {"k_prim": 32, "k_first": 144, "k_update": 240, "k_filter_x": 64,
+                   "k_filter_y": 64, "k_bc": 0, "k_stage_sin": 0}
+# FP64 operations per grid point of one launch (2 per DFMA, 1 per DADD/DMUL),
+# from the ncu instruction counts summarised in profiles/ (None: not yet
+# measured for that kernel).
+FP64_FLOP_PER_POINT: dict = {}
+FP64_PEAK_TFLOPS = 1.19   # measured DFMA throughput of this GB300 (profiles/fp64_peak.md)
+STEP_BYTES_FUSED_MIN = 1536  # compulsory bytes per point-step of a fused FP64 design, nk = 4
+
+
+def load_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (200 ms period)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-i", str(self.index), "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self._t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def build_case(args):
+    from navierstokes_gb300 import cases
+    return cases.stretched_ns_case(imax=args.imax, jmax=args.jmax, nk=args.nk)
+
+
+def workload_config(case, extra=None):
+    cfg = {"workload": f"Navier-Stokes {case.imax}x{case.jmax}, y stretched toward the "
+                       "centreline (eta = tanh(2.5y)/tanh(2.5)), M=0.5, Re=1000, Pr=0.72, "
+                       "pulse 1e-3 + isentropic vortex 0.1, D=40, sigma_f=0.2, "
+                       f"dt = min(CFL 0.5, viscous limit) = {case.dt:.4g}",
+           "imax": case.imax, "jmax": case.jmax, "nk": case.nk, "precision": "fp64",
+           "l2": "inputs larger than L2 (state and work arrays ~2 GB)",
+           "parallelism": "replicas only (one independent grid per GPU)"}
+    if extra:
+        cfg.update(extra)
+    return cfg
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "ours" else "gloo"
+        if backend == "nccl":
+            import torch
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+        pg = dist
+    return world, rank, local, pg
+
+
+def run_reference(args, world, rank):
+    """CPU oracle on all host threads; rank 0 only."""
+    if rank != 0:
+        return
+    import oracle
+    oracle.build()
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    case = build_case(args)
+    # one step of the full grid first, to size the sample
+    o = oracle.Oracle(case)
+    U = case.U0.copy()
+    t0 = time.perf_counter()
+    o.run(U, 0, 1)
+    t_full = time.perf_counter() - t0
+    budget = 150.0
+    jmax_s = case.jmax
+    if (args.steps + args.warmup) * t_full > budget:
+        frac = budget / ((args.steps + args.warmup) * t_full)
+        jmax_s = max(64, int(case.jmax * frac) // 16 * 16)
+    if jmax_s != case.jmax:
+        from navierstokes_gb300 import cases
+        o.close()
+        case = cases.stretched_ns_case(imax=case.imax, jmax=jmax_s, nk=case.nk)
+        o = oracle.Oracle(case)
+        U = case.U0.copy()
+    for it in range(args.warmup):
+        o.run(U, it, 1)
+    t0 = time.perf_counter()
+    for it in range(args.steps):
+        o.run(U, args.warmup + it, 1)
+    dt = time.perf_counter() - t0
+    val = case.points * args.steps / dt / 1e6
+    sample = (f"{args.steps} timed steps of a {case.imax}x{case.jmax} grid "
+              f"({'full grid' if jmax_s == args.jmax else 'rows cropped to bound the run'}), "
+              f"{threads} OpenMP threads")
+    line = {"metric": METRIC, "value": val, "unit": UNIT, "impl": "reference",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic: analytic pulse + isentropic vortex on the stretched grid",
+            "config": workload_config(case, {"full_jmax": args.jmax}),
+            "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline_sample(case, seconds=20.0):
+    """Oracle on the host cores, a bounded sample of the same workload."""
+    import oracle
+    oracle.build()
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    o = oracle.Oracle(case)
+    U = case.U0.copy()
+    t0 = time.perf_counter()
+    o.run(U, 0, 1)
+    t1 = time.perf_counter() - t0
+    n = max(1, min(8, int(seconds / max(t1, 1e-3))))
+    t0 = time.perf_counter()
+    o.run(U, 1, n)
+    dt = time.perf_counter() - t0
+    o.close()
+    return {"value": case.points * n / dt / 1e6, "unit": UNIT, "cores": threads,
+            "kind": "port",
+            "sample": f"{n} step(s) of the full {case.imax}x{case.jmax} grid after one "
+                      f"untimed step, C oracle (-O3, OpenMP over lines)"}
+
+
+def run_ours(args, world, rank, local, pg):
+    import torch
+    from navierstokes_gb300 import Solver
+    from navierstokes_gb300 import _lib as L
+
+    torch.cuda.set_device(local)
+    case = build_case(args)
+    solver = Solver(case, device=local)
+    # a stream of our own: the legacy default stream (handle 0) is not one the
+    # library can be handed, and events must sit on the launching stream
+    stream = torch.cuda.Stream()
+    solver.set_stream(stream.cuda_stream)
+    solver.set_state(case.U0)
+    launches = solver.launches_per_step()
+
+    def barrier():
+        if pg is not None:
+            pg.barrier()
+
+    for it in range(args.warmup):
+        solver.step(it, 1)
+    torch.cuda.synchronize()
+
+    # ---- device-resident throughput -------------------------------------
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    barrier()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for k in range(args.steps):
+        solver.step(args.warmup + k, 1)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clocks = sampler.stop()
+    ms = ev0.elapsed_time(ev1)
+    if pg is not None:
+        t = torch.tensor([ms], device=f"cuda:{local}")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    value = world * case.points * args.steps / (ms * 1e-3) / 1e6
+
+    # ---- per-kernel device times (events around each launch) ---------------
+    import ctypes as C
+    kms = (C.c_double * L.NS_KC_COUNT)()
+    kn = (C.c_int * L.NS_KC_COUNT)()
+    L.check(solver.lib.ns_time_kernels(solver._ctx, 10_000, 2, kms, kn), solver._ctx)
+    kernels = {}
+    for k in range(L.NS_KC_COUNT):
+        if kn[k]:
+            name = solver.lib.ns_kernel_name(k).decode()
+            kernels[name] = {"ms_per_launch": kms[k], "launches_per_step": kn[k],
+                             "share": 0.0}
+    tot = sum(v["ms_per_launch"] * v["launches_per_step"] for v in kernels.values())
+    for v in kernels.values():
+        v["share"] = v["ms_per_launch"] * v["launches_per_step"] / tot
+    dom = max(kernels, key=lambda n: kernels[n]["share"])
+    hbm_peak, peak_kind = load_peaks()
+    dms = kernels[dom]["ms_per_launch"]
+    bytes_launch = BYTES_PER_POINT.get(dom, 0) * case.points
+    achieved = bytes_launch / (dms * 1e-3) / 1e9
+    roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak,
+            "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": None,
+            "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})",
+            "bytes_per_launch": bytes_launch}
+    fl = FP64_FLOP_PER_POINT.get(dom)
+    if fl:
+        tf = fl * case.points / (dms * 1e-3) / 1e12
+        roof["fp64"] = {"achieved": tf, "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
+                        "frac": tf / FP64_PEAK_TFLOPS,
+                        "peak_source": "DFMA microbenchmark on this GB300 (profiles/fp64_peak.md)"}
+    step_bytes = STEP_BYTES_FUSED_MIN * case.points
+    roof["step_hbm_frac_fused_min"] = step_bytes / (ms_step * 1e-3) / 1e9 / hbm_peak
+
+    # ---- end to end through the C ABI with host buffers -----------------
+    Uh = torch.empty(case.U0.shape, dtype=torch.float64, pin_memory=True).numpy()
+    Uh[...] = case.U0
+    solver.set_stream(0)
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        solver.rk_euler(Uh, (k + 1) * case.dt, k)
+    t_e2e = time.perf_counter() - t0
+    if pg is not None:
+        t = torch.tensor([t_e2e], device=f"cuda:{local}")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        t_e2e = float(t.item())
+    e2e_val = world * case.points * args.steps / t_e2e / 1e6
+    nbytes = case.state_bytes()
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        try:
+            cpu = cpu_baseline_sample(case)
+        except Exception as e:  # the baseline must not kill the line
+            cpu = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                   "sample": f"failed: {e}"}
+    solver.close()
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64",
+                "data": "synthetic: analytic pulse + isentropic vortex on the stretched grid",
+                "config": workload_config(case),
+                "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": nbytes,
+                        "d2h_bytes_per_step": nbytes,
+                        "call": "ns_rk_euler (host U(nk,imax,jmax) in/out, one step per call)"},
+                "gpu_launches": launches * args.steps,
+                "roofline": roof, "kernels": kernels, "clocks": clocks}
+        if cpu is not None:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--imax", type=int, default=4096)
+    ap.add_argument("--jmax", type=int, default=2048)
+    ap.add_argument("--nk", type=int, default=4)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world, rank, local, pg = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        from navierstokes_gb300 import _build
+        _build.build()
+        run_ours(args, world, rank, local, pg)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -176,6 +176,28 @@ NS_API int ns_state_device(ns_ctx *ctx, void **dptr, int64_t *pitch);
 NS_API int ns_step_launches(ns_ctx *ctx, int *launches);
 NS_API int ns_filter_warmup(ns_ctx *ctx, int *warmup);
 
+/* Kernel classes of the step, for ns_time_kernels. */
+enum {
+    NS_KC_STAGE_SIN = 0, /* per-step source phase sin(wf*(iter+c_k)*dt) */
+    NS_KC_PRIM = 1,      /* T = gamma*p/rho, 1/rho                 (rhs.f90:20) */
+    NS_KC_FIRST = 2,     /* first derivatives, mu, k, tau, k*grad T (diff.f90,
+                            derivs.f90, coefficients.f90, eqeuler.f90:28-47) */
+    NS_KC_UPDATE = 3,    /* second derivatives, RHS, LDDRK update, buffer
+                            (eqeuler.f90:53-99, rk.f90:77-169) */
+    NS_KC_FILTER_X = 4,  /* lddfilterx                 (filtering.f90:9-96) */
+    NS_KC_FILTER_Y = 5,  /* lddfiltery                 (filtering.f90:98-190) */
+    NS_KC_BC = 6,        /* ccpml                      (cc.f90:6-68) */
+    NS_KC_COUNT = 7
+};
+
+/* Advances the state by `reps` steps from iter0, launching every kernel on
+ * its own (no graph) between CUDA events on the context stream, and writes
+ * per kernel class the mean device time of one launch in ms_per_launch[c]
+ * and the launches per step in launches[c] (arrays of NS_KC_COUNT). */
+NS_API int ns_time_kernels(ns_ctx *ctx, int iter0, int reps, double *ms_per_launch,
+                           int *launches);
+NS_API const char *ns_kernel_name(int kernel_class);
+
 #ifdef __cplusplus
 }
 #endif

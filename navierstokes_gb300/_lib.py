@@ -52,7 +52,11 @@ SIGNATURES = [
     ("ns_state_device", C.c_int, [_VP, C.POINTER(_VP), C.POINTER(C.c_int64)]),
     ("ns_step_launches", C.c_int, [_VP, C.POINTER(C.c_int)]),
     ("ns_filter_warmup", C.c_int, [_VP, C.POINTER(C.c_int)]),
+    ("ns_time_kernels", C.c_int, [_VP, C.c_int, C.c_int, _VP, _VP]),
+    ("ns_kernel_name", C.c_char_p, [C.c_int]),
 ]
+
+NS_KC_COUNT = 7
 
 
 class NsParams(C.Structure):

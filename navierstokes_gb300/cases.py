@@ -224,26 +224,47 @@ def acoustic_pulse_case(imax=201, jmax=201, nk=5, D=30, sigmaf=0.2, amp=0.01, ha
                 notes="Gaussian pulse, uniform grid (new initial-condition hook)")
 
 
+# Stability of the explicit step for the viscous terms: the LDDRK
+# amplification polynomial (rk.f90:27-46) stays within |G| <= 1 on the
+# negative real axis up to z = -4.071, and a diffusion operator built from two
+# DRP first derivatives (diff.f90:40-47) has eigenvalues down to
+# -2.703*nu/h^2 per direction.
+LDDRK_REAL_LIMIT = 4.071
+DRP_K2_MAX = 2.7034
+
+
+def viscous_dt(Re, Pr, inv_h2_sum, gamma=GAMMA, safety=0.5):
+    """Largest stable dt of the diffusion terms: the stress term diffuses
+    momentum with nu = (4/3)/Re and the heat-flux term of eqeuler.f90:90-91
+    diffuses pressure with gamma/(Re*Pr) (rho = T = 1)."""
+    nu = max(4.0 / 3.0 / Re, gamma / (Re * Pr))
+    return safety * LDDRK_REAL_LIMIT / (nu * DRP_K2_MAX * inv_h2_sum)
+
+
 def stretched_ns_case(imax=4096, jmax=2048, nk=4, D=40, sigmaf=0.2, mach=0.5, Re=1000.0,
                       Pr=0.72, pulse_amp=1e-3, pulse_cells=4.0, vortex_eps=0.1,
                       vortex_cells=6.0, vortex_upstream=200, cfl=0.5, steps=200, c1b=0.01,
                       c2b=20.0, beta=2.5, quirk_buffer=True):
-    """Navier-Stokes on a y-stretched grid: y(eta) = tanh(beta*eta)/tanh(beta),
-    eta uniform in [-1, 1] (the computational coordinate n(j)); the formula as
-    written clusters points toward y = +-1, so the centreline is the coarsest
-    row.  meshy(j) = d(eta)/dy times the buffer factor of init.f90:139-153,
-    applied to every y-derivative (NS_METRIC_EVERYWHERE).  x is uniform with
-    dx equal to the centreline dy.  Uniform mean flow u = mach, rho = 1,
-    p = 1/gamma; a pulse of half-width pulse_cells*dx at the centre and an
-    isentropic vortex of radius vortex_cells*dx, vortex_upstream cells
-    upstream."""
+    """Navier-Stokes on a y-grid stretched toward the centreline: the
+    computational coordinate eta = n(j), uniform in [-1, 1], is
+    eta = tanh(beta*y)/tanh(beta), i.e. y = atanh(eta*tanh(beta))/beta, so the
+    rows are finest at y = 0 (dy = deta*tanh(beta)/beta) and coarsest at
+    y = +-1.  meshy(j) = d(eta)/dy times the buffer factor of
+    init.f90:139-153, applied to every y-derivative (NS_METRIC_EVERYWHERE).
+    x is uniform with dx equal to the centreline dy.  Uniform mean flow
+    u = mach, rho = 1, p = 1/gamma; a pulse of half-width pulse_cells*dx at
+    the centre and an isentropic vortex of radius vortex_cells*dx,
+    vortex_upstream cells upstream.  dt is the smaller of the convective
+    CFL step and half the viscous stability limit (which binds at Re = 1000
+    on this grid)."""
     dn = 2.0 / (jmax - 1)
-    dx = dn * beta / math.tanh(beta)          # dy/d(eta) at eta = 0, times d(eta)
+    tb = math.tanh(beta)
+    dx = dn * tb / beta
     g = init_dados(imax, jmax, D, 0.0, dx * (imax - 1), -1.0, 1.0, c1b, c2b, quirk_buffer)
     eta = g["n"]
-    detady = math.tanh(beta) * np.cosh(beta * eta) ** 2 / beta
+    yphys = np.arctanh(np.clip(eta * tb, -1.0, 1.0)) / beta
+    detady = beta * (1.0 - (eta * tb) ** 2) / tb
     meshy = g["meshy"] * detady
-    yphys = np.tanh(beta * eta) / math.tanh(beta)
     X, Y = np.meshgrid(g["m"], yphys)
     xc = g["m"][imax // 2]
     psib = psi_profile(eta)
@@ -259,13 +280,16 @@ def stretched_ns_case(imax=4096, jmax=2048, nk=4, D=40, sigmaf=0.2, mach=0.5, Re
     U0[:, :, 2] = vv
     U0[:, :, 3] = vp + pp
     dy_min = float(np.min(np.diff(yphys)))
-    dt = cfl * min(dx / (abs(mach) + 1.0), dy_min / 1.0)
+    dt_conv = cfl * min(dx / (abs(mach) + 1.0), dy_min / 1.0)
+    inv_h2 = 1.0 / dx ** 2 + float(np.max(meshy / dn)) ** 2
+    dt = min(dt_conv, viscous_dt(Re, Pr, inv_h2))
     return Case(name=f"stretched_ns_{imax}x{jmax}", imax=imax, jmax=jmax, nk=nk, D=D, dt=dt,
                 dm=g["dm"], dn=g["dn"], sigmaf=sigmaf, m=g["m"], n=eta, meshx=g["meshx"],
                 meshy=meshy, sigmax=g["sigmax"], sigmay=g["sigmay"], Ub=Ub, rhob=rho0,
                 psib=psib, U0=U0, inviscid=False, metric_mode=L.NS_METRIC_EVERYWHERE, Re=Re,
                 Pr=Pr, steps=steps,
-                notes="y = tanh(2.5 eta)/tanh(2.5), pulse + isentropic vortex (new hook)")
+                notes="eta = tanh(2.5 y)/tanh(2.5) (finest at y = 0), pulse + isentropic "
+                      "vortex, dt = min(CFL 0.5, viscous limit) (new hook)")
 
 
 def params_from_case(case: Case, device: int = 0, precision: int = L.NS_PREC_FP64):

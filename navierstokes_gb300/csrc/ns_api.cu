@@ -639,4 +639,49 @@ int ns_filter_warmup(ns_ctx *c, int *warmup)
     return NS_OK;
 }
 
+int ns_time_kernels(ns_ctx *c, int iter0, int reps, double *ms, int *launches)
+{
+    if (!c || !ms || !launches || reps < 1)
+        return set_err(c, NS_ERR_PARAM, "ns_time_kernels: bad argument");
+    if (!c->have_state) return set_err(c, NS_ERR_STATE, "ns_time_kernels before ns_set_state");
+    NS_CUDA(c, cudaSetDevice(c->dev));
+    int cls[ns::kMaxStepLaunches], stage[ns::kMaxStepLaunches];
+    const int n = ns::step_sequence(c, cls, stage);
+    std::vector<cudaEvent_t> ev(n + 1);
+    for (auto &e : ev) NS_CUDA(c, cudaEventCreate(&e));
+    std::vector<double> tot(NS_KC_COUNT, 0.0);
+    for (int k = 0; k < NS_KC_COUNT; k++) launches[k] = 0;
+    for (int q = 0; q < n; q++) launches[cls[q]]++;
+    int rc = NS_OK;
+    if (c->src) {
+        cudaError_t e = ns::launch_set_iter(c->d_iter, iter0, c->stream);
+        if (e != cudaSuccess) rc = cuda_err(c, e, "set iter");
+    }
+    for (int r = 0; r < reps && rc == NS_OK; r++) {
+        cudaError_t e = cudaEventRecord(ev[0], c->stream);
+        for (int q = 0; q < n && e == cudaSuccess; q++) {
+            e = ns::launch_kernel(c, cls[q], stage[q], c->stream);
+            if (e == cudaSuccess) e = cudaEventRecord(ev[q + 1], c->stream);
+        }
+        if (e == cudaSuccess) e = cudaEventSynchronize(ev[n]);
+        for (int q = 0; q < n && e == cudaSuccess; q++) {
+            float t = 0.f;
+            e = cudaEventElapsedTime(&t, ev[q], ev[q + 1]);
+            tot[cls[q]] += t;
+        }
+        if (e != cudaSuccess) rc = cuda_err(c, e, "ns_time_kernels");
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    for (int k = 0; k < NS_KC_COUNT; k++)
+        ms[k] = launches[k] ? tot[k] / ((double)reps * launches[k]) : 0.0;
+    return rc;
+}
+
+const char *ns_kernel_name(int k)
+{
+    static const char *names[NS_KC_COUNT] = {"k_stage_sin", "k_prim",     "k_first", "k_update",
+                                             "k_filter_x",  "k_filter_y", "k_bc"};
+    return (k >= 0 && k < NS_KC_COUNT) ? names[k] : "";
+}
+
 }  // extern "C"

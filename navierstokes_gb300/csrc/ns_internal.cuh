@@ -100,7 +100,10 @@ struct ns_ctx {
 // Kernel launchers (ns_kernels.cu).  All enqueue on `s` and return the
 // launch status.
 namespace ns {
+constexpr int kMaxStepLaunches = 64;
 cudaError_t launch_step(ns_ctx *c, cudaStream_t s);
+cudaError_t launch_kernel(ns_ctx *c, int cls, int stage, cudaStream_t s);
+int step_sequence(const ns_ctx *c, int *cls, int *stage);
 cudaError_t launch_set_iter(int *d_iter, int iter, cudaStream_t s);
 cudaError_t launch_aos_to_soa(const double *in, double *out, const Dims &d, cudaStream_t s);
 cudaError_t launch_soa_to_aos(const double *in, double *out, const Dims &d, cudaStream_t s);

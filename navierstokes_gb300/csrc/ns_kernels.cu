@@ -495,72 +495,109 @@ static inline dim3 tile_grid(const Dims &d, dim3 blk)
     return dim3((d.imax + blk.x - 1) / blk.x, (d.jmax + blk.y - 1) / blk.y);
 }
 
+// One kernel of class `cls` (NS_KC_*) for `stage`.
 template <bool VISC, int NK>
-static cudaError_t launch_stage_t(ns_ctx *c, int stage, cudaStream_t s)
+static cudaError_t launch_kernel_t(ns_ctx *c, int cls, int stage, cudaStream_t s)
 {
     const Dims &d = c->d;
     const dim3 blk(32, 8);
     const dim3 grd = tile_grid(d, blk);
-    if (VISC) k_prim<<<grd, blk, 0, s>>>(d, c->U, c->aux, c->phys.gamma);
-    k_first<VISC, NK><<<grd, blk, 0, s>>>(d, c->U, c->dudm, c->dudn, c->aux, c->xcoef, c->ycoef,
-                                          c->phys);
-    StageCoef sc{c->alpha[stage], c->beta[stage], stage};
-    const bool src = c->src != nullptr;
-#define NS_UPD(FIRST, SRC)                                                                    \
-    k_update<VISC, NK, FIRST, SRC><<<grd, blk, 0, s>>>(d, c->U, c->W, c->dudm, c->dudn,       \
-                                                       c->aux, c->xcoef, c->ycoef, c->Ubase,  \
+    switch (cls) {
+    case NS_KC_PRIM:
+        k_prim<<<grd, blk, 0, s>>>(d, c->U, c->aux, c->phys.gamma);
+        break;
+    case NS_KC_FIRST:
+        k_first<VISC, NK><<<grd, blk, 0, s>>>(d, c->U, c->dudm, c->dudn, c->aux, c->xcoef,
+                                              c->ycoef, c->phys);
+        break;
+    case NS_KC_UPDATE: {
+        StageCoef sc{c->alpha[stage], c->beta[stage], stage};
+        const bool src = c->src != nullptr;
+#define NS_UPD(FIRST, SRC)                                                                     \
+    k_update<VISC, NK, FIRST, SRC><<<grd, blk, 0, s>>>(d, c->U, c->W, c->dudm, c->dudn,        \
+                                                       c->aux, c->xcoef, c->ycoef, c->Ubase,   \
                                                        c->sigx, c->sigy, c->src, c->stage_sin, \
                                                        c->phys, sc)
-    if (stage == 0) {
-        if (src) NS_UPD(true, true); else NS_UPD(true, false);
-    } else {
-        if (src) NS_UPD(false, true); else NS_UPD(false, false);
-    }
+        if (stage == 0) {
+            if (src) NS_UPD(true, true); else NS_UPD(true, false);
+        } else {
+            if (src) NS_UPD(false, true); else NS_UPD(false, false);
+        }
 #undef NS_UPD
-    {
+        break;
+    }
+    case NS_KC_FILTER_X: {
         const long long tx = (long long)d.jmax * d.nk * c->fx_chunks;
         k_filter<false><<<(unsigned)((tx + 127) / 128), 128, 0, s>>>(d, c->U, c->U2,
                                                                      c->fx_chunks, c->warm, c->fx);
+        break;
+    }
+    case NS_KC_FILTER_Y: {
         const long long ty = (long long)d.imax * d.nk * c->fy_chunks;
         k_filter<true><<<(unsigned)((ty + 127) / 128), 128, 0, s>>>(d, c->U2, c->U, c->fy_chunks,
                                                                     c->warm, c->fy);
+        break;
     }
-    {
+    case NS_KC_BC: {
         const int nt = d.imax > d.jmax ? d.imax : d.jmax;
         k_bc<<<(nt + 127) / 128, 128, 0, s>>>(d, c->U, c->rhob, c->psib, c->phys.gamma);
+        break;
     }
-    return cudaGetLastError();
-}
-
-static cudaError_t launch_stage(ns_ctx *c, int stage, cudaStream_t s)
-{
-    if (c->visc)
-        return c->d.nk == 5 ? launch_stage_t<true, 5>(c, stage, s)
-                            : launch_stage_t<true, 4>(c, stage, s);
-    return c->d.nk == 5 ? launch_stage_t<false, 5>(c, stage, s)
-                        : launch_stage_t<false, 4>(c, stage, s);
-}
-
-cudaError_t launch_step(ns_ctx *c, cudaStream_t s)
-{
-    if (c->src) {
+    case NS_KC_STAGE_SIN: {
         SinArgs a;
         a.wf = c->p.wf;
         a.dt = c->p.dt;
         for (int k = 0; k < 6; k++) a.ct[k] = c->ct[k];
         k_stage_sin<<<1, 32, 0, s>>>(c->d_iter, c->stage_sin, a);
+        break;
     }
-    for (int stage = 0; stage < 6; stage++) {
-        cudaError_t e = launch_stage(c, stage, s);
-        if (e != cudaSuccess) return e;
+    default:
+        return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
 }
 
+cudaError_t launch_kernel(ns_ctx *c, int cls, int stage, cudaStream_t s)
+{
+    if (c->visc)
+        return c->d.nk == 5 ? launch_kernel_t<true, 5>(c, cls, stage, s)
+                            : launch_kernel_t<true, 4>(c, cls, stage, s);
+    return c->d.nk == 5 ? launch_kernel_t<false, 5>(c, cls, stage, s)
+                        : launch_kernel_t<false, 4>(c, cls, stage, s);
+}
+
+// The launch sequence of one step (rk.f90:52-73): the source phase, then per
+// stage [prim], first, update, filter x, filter y, bc.
+int step_sequence(const ns_ctx *c, int *cls, int *stage)
+{
+    int n = 0;
+    if (c->src) { cls[n] = NS_KC_STAGE_SIN; stage[n++] = 0; }
+    for (int st = 0; st < 6; st++) {
+        if (c->visc) { cls[n] = NS_KC_PRIM; stage[n++] = st; }
+        cls[n] = NS_KC_FIRST; stage[n++] = st;
+        cls[n] = NS_KC_UPDATE; stage[n++] = st;
+        cls[n] = NS_KC_FILTER_X; stage[n++] = st;
+        cls[n] = NS_KC_FILTER_Y; stage[n++] = st;
+        cls[n] = NS_KC_BC; stage[n++] = st;
+    }
+    return n;
+}
+
+cudaError_t launch_step(ns_ctx *c, cudaStream_t s)
+{
+    int cls[kMaxStepLaunches], stage[kMaxStepLaunches];
+    const int n = step_sequence(c, cls, stage);
+    for (int q = 0; q < n; q++) {
+        cudaError_t e = launch_kernel(c, cls[q], stage[q], s);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 int count_step_launches(const ns_ctx *c)
 {
-    const int per_stage = (c->visc ? 1 : 0) + 1 + 1 + 2 + 1;
-    return 6 * per_stage + (c->src ? 1 : 0);
+    int cls[kMaxStepLaunches], stage[kMaxStepLaunches];
+    return step_sequence(c, cls, stage);
 }
 
 cudaError_t launch_set_iter(int *d_iter, int iter, cudaStream_t s)
