@@ -198,6 +198,42 @@ NS_API int ns_time_kernels(ns_ctx *ctx, int iter0, int reps, double *ms_per_laun
                            int *launches);
 NS_API const char *ns_kernel_name(int kernel_class);
 
+/*
+ * ns_step_noalloc -- the time step for callers that cannot allocate device
+ * memory.  No counterpart in the reference: it is an addition for hosts
+ * whose device memory belongs to something else (a framework or pool that
+ * hands out fixed buffers, a process under a hard memory cap where a
+ * cudaMalloc failure in the middle of a run is not acceptable, a caller that
+ * must not let an allocation synchronise the device between its own kernels).
+ *
+ * Advances the state U by nsteps calls of rk_euler (same kernels and results
+ * as ns_step) without calling cudaMalloc, cudaFree or any allocating
+ * library routine: every work array lives in one file-scope __device__
+ * array of NS_NOALLOC_MAX_BYTES, which every GPU that loads the library keeps
+ * until the process exits.  The caller passes the inputs and the output:
+ * p as for ns_create (host arrays, read on every call), and U, the device
+ * state: nk planes of jmax rows of `pitch` doubles (pitch >= imax, a
+ * multiple of 32), updated in place.  stream: a cudaStream_t, NULL for the
+ * default stream; the call returns once the work is enqueued.
+ *
+ * Limits: imax, jmax <= NS_NOALLOC_MAX_LINE and about (5*nk+9)*pitch*jmax
+ * doubles of work area (a 96x72 nk = 5 case uses 1.9 MB; 512x480 with
+ * nk = 4 fits); larger cases are rejected with NS_ERR_PARAM and a message
+ * giving the bytes needed.
+ *
+ * The first call on a device finds the work area's device address
+ * (cudaGetSymbolAddress, with that device current, which may also load the
+ * module): make that first call before any stream capture.  Every call
+ * shares the one work area and leaves its contents behind; each call writes
+ * every part it reads, so results never depend on an earlier call, but calls
+ * that overlap on the GPU (other streams, other host threads) race and must
+ * be serialised by the caller.
+ */
+#define NS_NOALLOC_MAX_BYTES (64u << 20)
+#define NS_NOALLOC_MAX_LINE 8192
+NS_API int ns_step_noalloc(const ns_params *p, double *U, int64_t pitch, int iter0, int nsteps,
+                           void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -244,6 +244,10 @@ int upload_field(ns_ctx *c, const double *h, int layout, double *dplanes)
 
 }  // namespace
 
+namespace ns {
+void record_error(const char *msg) { g_last_error = msg; }
+}  // namespace ns
+
 extern "C" {
 
 int ns_abi_version(void) { return NS_ABI_VERSION; }

@@ -112,4 +112,6 @@ cudaError_t launch_probes(const double *U, const Dims &d, int np, const int32_t 
 cudaError_t launch_count_nonfinite(const double *U, const Dims &d, unsigned long long *count,
                                    cudaStream_t s);
 int count_step_launches(const ns_ctx *c);
+// Makes msg the text ns_last_error(NULL) returns (ns_api.cu).
+void record_error(const char *msg);
 }  // namespace ns
