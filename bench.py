@@ -42,11 +42,18 @@ UNIT = "Mpt-steps/s"
 #   k_filter_*: U in, U out
 BYTES_PER_POINT = {"k_prim": 32, "k_first": 144, "k_update": 240, "k_filter_x": 64,
                    "k_filter_y": 64, "k_bc": 0, "k_stage_sin": 0}
-# FP64 operations per grid point of one launch (2 per DFMA, 1 per DADD/DMUL),
-# from the ncu instruction counts summarised in profiles/ (None: not yet
-# measured for that kernel).
-FP64_FLOP_PER_POINT: dict = {}
-FP64_PEAK_TFLOPS = 1.19   # measured DFMA throughput of this GB300 (profiles/fp64_peak.md)
+# FP64 work per grid point of one launch, from the ncu instruction counts of
+# profiles/fp64_counts_ns_2048x2048.md (nk = 4, Navier-Stokes): flops (2 per
+# DFMA, 1 per DADD/DMUL) and FP64-pipe thread instructions.
+FP64_FLOP_PER_POINT = {"k_prim": 12.0, "k_first": 219.15, "k_update": 111.45,
+                       "k_filter_x": 86.71, "k_filter_y": 86.71}
+FP64_INST_PER_POINT = {"k_prim": 7.0, "k_first": 142.03, "k_update": 74.82,
+                       "k_filter_x": 56.33, "k_filter_y": 56.33}
+# DRAM bytes (read + write) per point of one launch from the same capture
+# (2048x2048), scaled to a launch by the number of points.
+TRAFFIC_PER_POINT = {"k_prim": 21.4, "k_first": 130.8, "k_update": 230.6,
+                     "k_filter_x": 59.5, "k_filter_y": 59.5}
+FP64_PEAK_FALLBACK_TFLOPS = 1.19  # DFMA throughput measured on the GB300s
 STEP_BYTES_FUSED_MIN = 1536  # compulsory bytes per point-step of a fused FP64 design, nk = 4
 
 
@@ -283,16 +290,32 @@ def run_ours(args, world, rank, local, pg):
     dms = kernels[dom]["ms_per_launch"]
     bytes_launch = BYTES_PER_POINT.get(dom, 0) * case.points
     achieved = bytes_launch / (dms * 1e-3) / 1e9
+    trafficpp = TRAFFIC_PER_POINT.get(dom)
     roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak,
-            "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": None,
+            "unit": "GB/s", "frac": achieved / hbm_peak,
+            "traffic": trafficpp * case.points if trafficpp else None,
+            "traffic_source": "ncu dram__bytes_read+write per point of a 2048x2048 capture, "
+                              "times the points of this launch",
             "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})",
             "bytes_per_launch": bytes_launch}
+    fp64_peak = C.c_double(0.0)
+    if solver.lib.ns_fp64_peak(local, C.byref(fp64_peak)) != 0 or fp64_peak.value <= 0:
+        fp64_peak.value = FP64_PEAK_FALLBACK_TFLOPS
+    for name, v in kernels.items():
+        fl = FP64_FLOP_PER_POINT.get(name)
+        if fl:
+            v["fp64_tflops"] = fl * case.points / (v["ms_per_launch"] * 1e-3) / 1e12
+            v["fp64_frac"] = v["fp64_tflops"] / fp64_peak.value
     fl = FP64_FLOP_PER_POINT.get(dom)
     if fl:
         tf = fl * case.points / (dms * 1e-3) / 1e12
-        roof["fp64"] = {"achieved": tf, "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
-                        "frac": tf / FP64_PEAK_TFLOPS,
-                        "peak_source": "DFMA microbenchmark on this GB300 (profiles/fp64_peak.md)"}
+        ins = FP64_INST_PER_POINT[dom] * case.points / (dms * 1e-3) / 1e9
+        peak_ins = fp64_peak.value * 1e3 / 2.0
+        roof["fp64"] = {"achieved": tf, "peak": fp64_peak.value, "unit": "TFLOP/s",
+                        "frac": tf / fp64_peak.value, "flop_per_point": fl,
+                        "pipe_inst_per_s": ins * 1e9, "pipe_frac": ins / peak_ins,
+                        "peak_source": "ns_fp64_peak(): DFMA loop measured live on this GPU",
+                        "binding": "the FP64 pipe binds this kernel, not HBM"}
     step_bytes = STEP_BYTES_FUSED_MIN * case.points
     roof["step_hbm_frac_fused_min"] = step_bytes / (ms_step * 1e-3) / 1e9 / hbm_peak
 

@@ -198,6 +198,11 @@ NS_API int ns_time_kernels(ns_ctx *ctx, int iter0, int reps, double *ms_per_laun
                            int *launches);
 NS_API const char *ns_kernel_name(int kernel_class);
 
+/* Library diagnostic, no counterpart in the reference: measured FP64 FMA
+ * throughput of `device` in TFLOP/s (2 flops per DFMA), the bound of the
+ * FP64 stage kernels on GB300. */
+NS_API int ns_fp64_peak(int device, double *tflops);
+
 /*
  * ns_step_noalloc -- the time step for callers that cannot allocate device
  * memory.  No counterpart in the reference: it is an addition for hosts

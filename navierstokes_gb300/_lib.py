@@ -54,6 +54,7 @@ SIGNATURES = [
     ("ns_filter_warmup", C.c_int, [_VP, C.POINTER(C.c_int)]),
     ("ns_time_kernels", C.c_int, [_VP, C.c_int, C.c_int, _VP, _VP]),
     ("ns_kernel_name", C.c_char_p, [C.c_int]),
+    ("ns_fp64_peak", C.c_int, [C.c_int, C.POINTER(C.c_double)]),
     ("ns_step_noalloc", C.c_int, [_VP, _VP, C.c_int64, C.c_int, C.c_int, _VP]),
 ]
 

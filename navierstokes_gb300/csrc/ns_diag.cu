@@ -1,0 +1,64 @@
+// ns_diag.cu -- library diagnostics with no counterpart in the reference.
+//
+// ns_fp64_peak: the FP64 FMA throughput of a device, measured with a
+// register-only DFMA loop (8 independent chains per thread, 4 blocks of 256
+// threads per SM).  On GB300 the FP64 pipe, not HBM, bounds the FP64 stage
+// kernels, so this is the denominator of their FP64 roofline fraction.
+#include "ns_internal.cuh"
+
+namespace {
+
+__device__ double g_peak_sink[1];
+
+__global__ void k_dfma_loop(int iters, double a, double b)
+{
+    double x[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) x[q] = threadIdx.x * 1e-9 + q;
+    for (int it = 0; it < iters; it++) {
+#pragma unroll
+        for (int q = 0; q < 8; q++) x[q] = fma(x[q], a, b);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int q = 0; q < 8; q++) s += x[q];
+    if (s == 12345.678) g_peak_sink[0] = s;  // keeps the loop; never true
+}
+
+}  // namespace
+
+extern "C" int ns_fp64_peak(int device, double *tflops)
+{
+    if (!tflops) return NS_ERR_PARAM;
+    *tflops = 0.0;
+    if (cudaSetDevice(device) != cudaSuccess) return NS_ERR_CUDA;
+    int nsm = 0;
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
+        return NS_ERR_CUDA;
+    const int blocks = nsm * 4, threads = 256, iters = 4096;
+    cudaEvent_t e0, e1;
+    if (cudaEventCreate(&e0) != cudaSuccess) return NS_ERR_CUDA;
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return NS_ERR_CUDA;
+    }
+    int rc = NS_OK;
+    double best = 0.0;
+    k_dfma_loop<<<blocks, threads>>>(64, 0.999, 1e-3);
+    for (int r = 0; r < 3 && rc == NS_OK; r++) {
+        cudaEventRecord(e0, 0);
+        k_dfma_loop<<<blocks, threads>>>(iters, 0.999, 1e-3);
+        cudaEventRecord(e1, 0);
+        if (cudaEventSynchronize(e1) != cudaSuccess) { rc = NS_ERR_CUDA; break; }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        const double flops = 2.0 * blocks * threads * (double)iters * 8.0;
+        const double tf = flops / (ms * 1e-3) / 1e12;
+        if (tf > best) best = tf;
+    }
+    if (cudaGetLastError() != cudaSuccess) rc = NS_ERR_CUDA;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *tflops = best;
+    return rc;
+}
