@@ -56,7 +56,9 @@ enum {
 /* Arithmetic of the stage loop. */
 enum {
     NS_PREC_FP64 = 0,  /* plain FP64, the reference's arithmetic */
-    NS_PREC_SPLIT = 1  /* FP64 mean flow + FP32 perturbation state */
+    NS_PREC_SPLIT = 1  /* FP64 mean flow + FP32 perturbation state; Euler
+                          (inviscid = 1), nk = 4, base flow Ub uniform in x
+                          with v = 0 and uniform p */
 };
 
 /* Acoustic source of rk.f90:171-193. */
@@ -187,7 +189,12 @@ enum {
     NS_KC_FILTER_X = 4,  /* lddfilterx                 (filtering.f90:9-96) */
     NS_KC_FILTER_Y = 5,  /* lddfiltery                 (filtering.f90:98-190) */
     NS_KC_BC = 6,        /* ccpml                      (cc.f90:6-68) */
-    NS_KC_COUNT = 7
+    NS_KC_SPLIT_STAGE = 7, /* split precision: fused FP32 derivatives, RHS,
+                              FP64 LDDRK update, buffer (rk.f90:52-64) */
+    NS_KC_SPLIT_FX = 8,  /* split precision: lddfilterx on the FP32 perturbation */
+    NS_KC_SPLIT_FY = 9,  /* split precision: lddfiltery on the FP32 perturbation */
+    NS_KC_SPLIT_BC = 10, /* split precision: ccpml on the perturbation */
+    NS_KC_COUNT = 11
 };
 
 /* Advances the state by `reps` steps from iter0, launching every kernel on

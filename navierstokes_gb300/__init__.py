@@ -7,8 +7,8 @@ and the reference-shaped solver interface (`Solver`).
 """
 from . import _lib
 from .cases import (Case, acoustic_pulse_case, init_dados, mixing_layer_case,
-                    stretched_ns_case)
+                    stretched_ns_case, uniform_flow_case)
 from .solver import Solver
 
 __all__ = ["Case", "Solver", "acoustic_pulse_case", "init_dados", "mixing_layer_case",
-           "stretched_ns_case", "_lib"]
+           "stretched_ns_case", "uniform_flow_case", "_lib"]

@@ -58,7 +58,7 @@ SIGNATURES = [
     ("ns_step_noalloc", C.c_int, [_VP, _VP, C.c_int64, C.c_int, C.c_int, _VP]),
 ]
 
-NS_KC_COUNT = 7
+NS_KC_COUNT = 11
 
 
 class NsParams(C.Structure):

@@ -241,6 +241,40 @@ def viscous_dt(Re, Pr, inv_h2_sum, gamma=GAMMA, safety=0.5):
     return safety * LDDRK_REAL_LIMIT / (nu * DRP_K2_MAX * inv_h2_sum)
 
 
+def uniform_flow_case(imax=4096, jmax=4096, nk=4, D=30, sigmaf=0.2, mach=0.5, pulse_amp=1e-4,
+                      pulse_halfwidth=3.0, vortex_eps=1e-3, vortex_radius=6.0,
+                      vortex_upstream=200, cfl=0.5, steps=1000, c1b=0.01, c2b=20.0,
+                      quirk_buffer=True, inviscid=True, Re=1000.0, Pr=0.72):
+    """Euler on a uniform grid (dx = dy = 1, centred on the origin) with a
+    uniform mean flow u = mach, rho = 1, p = 1/gamma, a Gaussian pulse
+    p' = rho' = pulse_amp*exp(-ln2*r^2/b^2) at the centre and a Gaussian
+    isentropic vortex of strength vortex_eps and radius vortex_radius cells
+    vortex_upstream cells upstream; dt = cfl*dx/(|u|+c).  With the default
+    sizes this is the split-precision workload: the acoustic-pulse case
+    scaled to 4096x4096 at M = 0.5 with small perturbations."""
+    hx, hy = (imax - 1) / 2.0, (jmax - 1) / 2.0
+    g = init_dados(imax, jmax, D, -hx, hx, -hy, hy, c1b, c2b, quirk_buffer)
+    X, Y = np.meshgrid(g["m"], g["n"])
+    rho0 = np.ones(jmax)
+    psib = psi_profile(g["n"])
+    Ub = base_field(imax, nk, rho0, np.full(jmax, mach), np.zeros(jmax),
+                    np.full(jmax, 1.0 / GAMMA), psib)
+    U0 = Ub.copy()
+    pp = _pulse(X, Y, 0.0, 0.0, pulse_amp, pulse_halfwidth)
+    vr, vu, vv, vp = _isentropic_vortex(X, Y, -float(vortex_upstream), 0.0, vortex_eps,
+                                        vortex_radius)
+    U0[:, :, 0] = vr + pp
+    U0[:, :, 1] = mach + vu
+    U0[:, :, 2] = vv
+    U0[:, :, 3] = vp + pp
+    dt = cfl * min(g["dm"], g["dn"]) / (abs(mach) + 1.0)
+    return Case(name=f"uniform_flow_{imax}x{jmax}", imax=imax, jmax=jmax, nk=nk, D=D, dt=dt,
+                dm=g["dm"], dn=g["dn"], sigmaf=sigmaf, m=g["m"], n=g["n"], meshx=g["meshx"],
+                meshy=g["meshy"], sigmax=g["sigmax"], sigmay=g["sigmay"], Ub=Ub, rhob=rho0,
+                psib=psib, U0=U0, inviscid=inviscid, Re=Re, Pr=Pr, steps=steps,
+                notes="uniform mean flow, pulse + isentropic vortex (new hook)")
+
+
 def stretched_ns_case(imax=4096, jmax=2048, nk=4, D=40, sigmaf=0.2, mach=0.5, Re=1000.0,
                       Pr=0.72, pulse_amp=1e-3, pulse_cells=4.0, vortex_eps=0.1,
                       vortex_cells=6.0, vortex_upstream=200, cfl=0.5, steps=200, c1b=0.01,

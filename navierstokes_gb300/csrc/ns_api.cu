@@ -148,6 +148,63 @@ int filter_warmup(double sigmaf)
     return w;
 }
 
+// Warm-up for a given decay threshold (2^-60 for FP64 results, 2^-32 for
+// the FP32 perturbation filters).
+int filter_warmup_thresh(double sigmaf, double thresh)
+{
+    const int kMax = 4096;
+    int worst = 0;
+    std::vector<double> e(kMax + 6);
+    for (int u = 0; u < 6; u++) {
+        std::fill(e.begin(), e.end(), 0.0);
+        e[u] = 1.0;
+        int last_big = 0;
+        for (int q = 6; q < kMax + 6; q++) {
+            double v = 0.0;
+            for (int s = 1; s <= 6; s++) v += -sigmaf * kDf[s] * e[q - s];
+            e[q] = v;
+            if (std::fabs(v) >= thresh) last_big = q - 5;
+        }
+        if (last_big >= kMax - 64) return -1;
+        if (last_big > worst) worst = last_big;
+    }
+    const int w = worst + 8;
+    return w < 16 ? 16 : w;
+}
+
+// The three in-place sweeps of lddfilterx/lddfiltery (filtering.f90:39-94)
+// on one line, serially, in FP64.
+void serial_filter_line(double *u, int n, double sigmaf, const double *dfb)
+{
+    for (int q = 1; q <= 6; q++) {
+        double Du = 0.0;
+        for (int s = -1; s <= 5; s++) Du += dfb[s + 1] * u[q + s];
+        u[q] -= sigmaf * Du;
+    }
+    for (int q = 6; q <= n - 7; q++) {
+        double Du = 0.0;
+        for (int s = -6; s <= 6; s++) Du += kDf[s < 0 ? -s : s] * u[q + s];
+        u[q] -= sigmaf * Du;
+    }
+    for (int q = n - 2; q >= n - 7; q--) {
+        double Du = 0.0;
+        for (int s = -1; s <= 5; s++) Du += dfb[s + 1] * u[q - s];
+        u[q] -= sigmaf * Du;
+    }
+}
+
+// DRP first derivative of a line with the per-position table (FP64).
+double line_derivative(const double *f, int q, int n, const double *c)
+{
+    if (q >= 3 && q < n - 3)
+        return c[4] * (f[q + 1] - f[q - 1]) + c[5] * (f[q + 2] - f[q - 2]) +
+               c[6] * (f[q + 3] - f[q - 3]);
+    const int o0 = (q < 3) ? -q : (n - 7 - q);
+    double r = 0.0;
+    for (int z = 0; z < 7; z++) r += c[z] * f[q + o0 + z];
+    return r;
+}
+
 int choose_chunks(int nlines_total, int n, int warm, int target_threads)
 {
     if (warm < 0) return 1;
@@ -157,6 +214,18 @@ int choose_chunks(int nlines_total, int n, int warm, int target_threads)
     if (c > maxc) c = maxc;
     if (c < 1) c = 1;
     return c;
+}
+
+template <class T>
+int dalloc(ns_ctx *c, T **p, size_t count);
+
+template <class T>
+int upload_vec(ns_ctx *c, T *dst, const std::vector<T> &v)
+{
+    cudaError_t e = cudaMemcpyAsync(dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice,
+                                    c->stream);
+    if (e != cudaSuccess) return cuda_err(c, e, "upload");
+    return NS_OK;
 }
 
 template <class T>
@@ -173,6 +242,13 @@ int dalloc(ns_ctx *c, T **p, size_t count)
 
 void free_all(ns_ctx *c)
 {
+    {
+        ns::SplitState &sp = c->sp;
+        float *fb[] = {sp.q[0], sp.q[1], sp.xc, sp.yc, sp.xcl, sp.ycl, sp.sigx, sp.sigy, sp.src,
+                       sp.rho_bc, sp.ycorr, sp.mean_buf};
+        for (float *b : fb)
+            if (b) cudaFree(b);
+    }
     if (c->step_exec) cudaGraphExecDestroy(c->step_exec);
     double *bufs[] = {c->U,    c->U2,   c->W,     c->dudm, c->dudn, c->aux,
                       c->Ubase, c->src, c->xcoef, c->ycoef, c->sigx, c->sigy,
@@ -202,8 +278,12 @@ int validate(const ns_params *p)
         return set_err(nullptr, NS_ERR_PARAM, "D=%d: need 0 <= 2*D <= min(imax,jmax)", p->D);
     if (p->metric_mode != NS_METRIC_BANDS && p->metric_mode != NS_METRIC_EVERYWHERE)
         return set_err(nullptr, NS_ERR_PARAM, "metric_mode=%d", p->metric_mode);
-    if (p->precision != NS_PREC_FP64)
+    if (p->precision != NS_PREC_FP64 && p->precision != NS_PREC_SPLIT)
         return set_err(nullptr, NS_ERR_UNSUPPORTED, "precision=%d is not available", p->precision);
+    if (p->precision == NS_PREC_SPLIT && (!p->inviscid || p->nk != 4))
+        return set_err(nullptr, NS_ERR_UNSUPPORTED,
+                       "split precision is implemented for the Euler equations (inviscid=1) "
+                       "with nk=4; got inviscid=%d nk=%d", p->inviscid, p->nk);
     if (p->source_mode < NS_SRC_NONE || p->source_mode > NS_SRC_FIELD)
         return set_err(nullptr, NS_ERR_PARAM, "source_mode=%d", p->source_mode);
     if (!(p->dt > 0) || !(p->dm > 0) || !(p->dn > 0) || !(p->gamma > 1.0))
@@ -239,6 +319,117 @@ int upload_field(ns_ctx *c, const double *h, int layout, double *dplanes)
     } else {
         return set_err(c, NS_ERR_PARAM, "layout=%d", layout);
     }
+    return NS_OK;
+}
+
+// Split precision: FP64 base flow + FP32 perturbation (ns_split.cu).
+int create_split(ns_ctx *c)
+{
+    const ns_params *p = &c->p;
+    const ns::Dims &d = c->d;
+    ns::SplitState &sp = c->sp;
+    const int imax = d.imax, jmax = d.jmax, nk = d.nk;
+    auto ub = [&](int k, int i, int j) -> double {
+        return p->ub_layout == NS_LAYOUT_FORTRAN
+                   ? p->Ub[k + (size_t)nk * (i + (size_t)imax * j)]
+                   : p->Ub[((size_t)k * jmax + j) * imax + i];
+    };
+    std::vector<double> rho(jmax), uu(jmax);
+    const double pb = ub(3, 0, 0);
+    for (int j = 0; j < jmax; j++) {
+        rho[j] = ub(0, 0, j);
+        uu[j] = ub(1, 0, j);
+        for (int i = 0; i < imax; i++) {
+            if (ub(0, i, j) != rho[j] || ub(1, i, j) != uu[j] || ub(2, i, j) != 0.0 ||
+                ub(3, i, j) != pb)
+                return set_err(c, NS_ERR_UNSUPPORTED,
+                               "split precision needs a base flow uniform in x with v = 0 and "
+                               "uniform p (violated at i=%d j=%d)", i + 1, j + 1);
+        }
+    }
+    sp.fpitch = (imax + 31) / 32 * 32;
+    const size_t P = (size_t)d.plane, FP = (size_t)sp.fpitch * jmax;
+    int rc;
+    if ((rc = dalloc(c, &c->U, nk * P)) || (rc = dalloc(c, &c->U2, nk * P)) ||
+        (rc = dalloc(c, &c->W, nk * P)) || (rc = dalloc(c, &c->Ubase, nk * P)) ||
+        (rc = dalloc(c, &sp.q[0], 4 * FP)) || (rc = dalloc(c, &sp.q[1], 4 * FP)) ||
+        (rc = dalloc(c, &sp.xc, (size_t)ns::kCoefStride * imax)) ||
+        (rc = dalloc(c, &sp.yc, (size_t)ns::kCoefStride * jmax)) ||
+        (rc = dalloc(c, &sp.xcl, (size_t)ns::kCoefStride * imax)) ||
+        (rc = dalloc(c, &sp.ycl, (size_t)ns::kCoefStride * jmax)) ||
+        (rc = dalloc(c, &sp.sigx, (size_t)imax)) || (rc = dalloc(c, &sp.sigy, (size_t)jmax)) ||
+        (rc = dalloc(c, &sp.rho_bc, (size_t)jmax)) || (rc = dalloc(c, &sp.ycorr, 4 * (size_t)jmax)) ||
+        (rc = dalloc(c, &sp.mean_buf, 4 * (size_t)jmax)) ||
+        (rc = dalloc(c, &c->stage_sin, 8)) || (rc = dalloc(c, &c->d_iter, 1)) ||
+        (rc = dalloc(c, &c->d_count, 1)))
+        return rc;
+    if (p->source_mode != NS_SRC_NONE && (rc = dalloc(c, &sp.src, FP))) return rc;
+    cudaError_t e = cudaMemsetAsync(sp.q[0], 0, 4 * FP * sizeof(float), c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(sp.q[1], 0, 4 * FP * sizeof(float), c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->W, 0, nk * P * sizeof(double), c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->d_iter, 0, sizeof(int), c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->stage_sin, 0, 8 * sizeof(double), c->stream);
+    if (e != cudaSuccess) return cuda_err(c, e, "cudaMemset");
+
+    std::vector<double> tx, ty;
+    build_coef(tx, imax, p->dm, p->meshx, d.D, p->metric_mode);
+    build_coef(ty, jmax, p->dn, p->meshy, d.D, p->metric_mode);
+    std::vector<float> txf(tx.begin(), tx.end()), tyf(ty.begin(), ty.end());
+    std::vector<float> txl(tx.size()), tyl(ty.size());
+    for (size_t q = 0; q < tx.size(); q++) txl[q] = (float)(tx[q] - (double)txf[q]);
+    for (size_t q = 0; q < ty.size(); q++) tyl[q] = (float)(ty[q] - (double)tyf[q]);
+    std::vector<float> sx(p->sigmax, p->sigmax + imax), sy(p->sigmay, p->sigmay + jmax);
+    // base-flow quantities (FP64, rounded once)
+    std::vector<float> mean(4 * (size_t)jmax), rbc(jmax), corr(4 * (size_t)jmax, 0.f);
+    for (int j = 0; j < jmax; j++) {
+        mean[j] = (float)rho[j];
+        mean[jmax + j] = (float)uu[j];
+        mean[2 * jmax + j] = (float)line_derivative(rho.data(), j, jmax, &ty[(size_t)j * ns::kCoefStride]);
+        mean[3 * jmax + j] = (float)line_derivative(uu.data(), j, jmax, &ty[(size_t)j * ns::kCoefStride]);
+        rbc[j] = (float)(p->rhob[j] - rho[j]);
+    }
+    {
+        // action of the y filter (REAL(4) boundary coefficients) on Ub
+        std::vector<double> col(jmax), f(jmax);
+        for (int k = 0; k < 4; k++) {
+            for (int j = 0; j < jmax; j++) col[j] = (k == 0) ? rho[j] : (k == 1) ? uu[j] : (k == 2) ? 0.0 : pb;
+            f = col;
+            serial_filter_line(f.data(), jmax, p->sigmaf, kDfbY);
+            for (int j = 0; j < jmax; j++) corr[(size_t)k * jmax + j] = (float)(f[j] - col[j]);
+        }
+    }
+    if ((rc = upload_vec(c, sp.xc, txf)) || (rc = upload_vec(c, sp.yc, tyf)) ||
+        (rc = upload_vec(c, sp.xcl, txl)) || (rc = upload_vec(c, sp.ycl, tyl)) ||
+        (rc = upload_vec(c, sp.sigx, sx)) || (rc = upload_vec(c, sp.sigy, sy)) ||
+        (rc = upload_vec(c, sp.mean_buf, mean)) || (rc = upload_vec(c, sp.rho_bc, rbc)) ||
+        (rc = upload_vec(c, sp.ycorr, corr)))
+        return rc;
+    std::vector<float> field;
+    if (p->source_mode != NS_SRC_NONE) {
+        field.assign(FP, 0.f);
+        for (int j = 0; j < jmax; j++)
+            for (int i = 0; i < imax; i++) {
+                double v;
+                if (p->source_mode == NS_SRC_GAUSSIAN) {
+                    const double dx = p->m[i] - p->m_pt, dy = p->n[j] - p->n_pt;
+                    v = p->amplitude * std::exp(-(std::log(2.0) * (dx * dx + dy * dy) / (p->r0 * p->r0)));
+                } else {
+                    v = p->src_field[(size_t)j * imax + i];
+                }
+                field[(size_t)j * sp.fpitch + i] = (float)v;
+            }
+        if ((rc = upload_vec(c, sp.src, field))) return rc;
+    }
+    if ((rc = upload_field(c, p->Ub, p->ub_layout, c->Ubase))) return rc;
+    e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_err(c, e, "split setup");
+    sp.mean.rho = sp.mean_buf;
+    sp.mean.u = sp.mean_buf + jmax;
+    sp.mean.drho = sp.mean_buf + 2 * jmax;
+    sp.mean.du = sp.mean_buf + 3 * jmax;
+    sp.mean.p = (float)pb;
+    sp.mean.gamma = (float)p->gamma;
+    sp.p_bc = (float)(1.0 / p->gamma - pb);
     return NS_OK;
 }
 
@@ -324,12 +515,17 @@ int ns_create(const ns_params *p, ns_ctx **out)
     d.plane = (long long)d.pitch * d.jmax;
     c->visc = !p->inviscid;
     const size_t P = (size_t)d.plane, nk = (size_t)d.nk;
+    c->split = (p->precision == NS_PREC_SPLIT);
 
 #define NS_TRY(x)                     \
     do {                              \
         rc = (x);                     \
         if (rc != NS_OK) goto fail;   \
     } while (0)
+    if (c->split) {
+        NS_TRY(create_split(c));
+        goto constants;
+    }
     NS_TRY(dalloc(c, &c->U, nk * P));
     NS_TRY(dalloc(c, &c->U2, nk * P));
     NS_TRY(dalloc(c, &c->W, nk * P));
@@ -409,6 +605,7 @@ int ns_create(const ns_params *p, ns_ctx **out)
     }
 
     // constants
+constants:
     {
         ns::Physics &ph = c->phys;
         ph.gamma = p->gamma;
@@ -446,6 +643,15 @@ int ns_create(const ns_params *p, ns_ctx **out)
         const int target = nsm * 4 * 2 * 32;  // about two warps per SM sub-partition
         c->fx_chunks = choose_chunks(d.jmax * d.nk, d.imax, c->warm, target);
         c->fy_chunks = choose_chunks(d.imax * d.nk, d.jmax, c->warm, target);
+        if (c->split) {
+            // FP32 filters are bound by memory: aim at 32 resident warps per SM
+            ns::SplitState &sp = c->sp;
+            sp.warm = filter_warmup_thresh(p->sigmaf, std::ldexp(1.0, -32));
+            const int twarps = nsm * 32;
+            const int xgroups = 4 * ((d.jmax + 31) / 32);
+            sp.fx_chunks = choose_chunks(xgroups, d.imax, sp.warm, twarps);
+            sp.fy_chunks = choose_chunks(d.imax * 4, d.jmax, sp.warm, twarps * 32);
+        }
         c->launches_per_step = ns::count_step_launches(c);
     }
 #undef NS_TRY
@@ -476,6 +682,7 @@ int ns_set_state(ns_ctx *c, const double *U, int layout)
     NS_CUDA(c, cudaSetDevice(c->dev));
     int rc = upload_field(c, U, layout, c->U);
     if (rc != NS_OK) return rc;
+    if (c->split) NS_CUDA(c, ns::launch_split_from_full(c, c->U, c->stream));
     NS_CUDA(c, cudaStreamSynchronize(c->stream));
     c->have_state = true;
     return NS_OK;
@@ -488,6 +695,7 @@ int ns_get_state(ns_ctx *c, double *U, int layout)
     NS_CUDA(c, cudaSetDevice(c->dev));
     const ns::Dims &d = c->d;
     const size_t row = (size_t)d.imax * sizeof(double);
+    if (c->split) NS_CUDA(c, ns::launch_split_to_full(c, c->U, c->stream));
     if (layout == NS_LAYOUT_SOA) {
         NS_CUDA(c, cudaMemcpy2DAsync(U, row, c->U, d.pitch * sizeof(double), row,
                                      (size_t)d.jmax * d.nk, cudaMemcpyDeviceToHost, c->stream));
@@ -534,7 +742,7 @@ int ns_step(ns_ctx *c, int iter0, int nsteps)
     NS_CUDA(c, cudaSetDevice(c->dev));
     int rc = ensure_graph(c);
     if (rc != NS_OK) return rc;
-    if (c->src) NS_CUDA(c, ns::launch_set_iter(c->d_iter, iter0, c->stream));
+    if (c->src || c->sp.src) NS_CUDA(c, ns::launch_set_iter(c->d_iter, iter0, c->stream));
     for (int s = 0; s < nsteps; s++) NS_CUDA(c, cudaGraphLaunch(c->step_exec, c->stream));
     return NS_OK;
 }
@@ -585,6 +793,7 @@ int ns_get_probes(ns_ctx *c, int np, const int32_t *pi, const int32_t *pj, doubl
     }
     NS_CUDA(c, cudaMemcpyAsync(c->probe_idx, idx.data(), idx.size() * sizeof(int32_t),
                                cudaMemcpyHostToDevice, c->stream));
+    if (c->split) NS_CUDA(c, ns::launch_split_to_full(c, c->U, c->stream));
     NS_CUDA(c, ns::launch_probes(c->U, c->d, np, c->probe_idx, c->probe_buf, c->stream));
     NS_CUDA(c, cudaMemcpyAsync(out, c->probe_buf, (size_t)np * c->d.nk * sizeof(double),
                                cudaMemcpyDeviceToHost, c->stream));
@@ -599,6 +808,7 @@ int ns_check_finite(ns_ctx *c, int64_t *nonfinite)
     NS_CUDA(c, cudaSetDevice(c->dev));
     unsigned long long h = 0;
     NS_CUDA(c, cudaMemsetAsync(c->d_count, 0, sizeof(unsigned long long), c->stream));
+    if (c->split) NS_CUDA(c, ns::launch_split_to_full(c, c->U, c->stream));
     NS_CUDA(c, ns::launch_count_nonfinite(c->U, c->d, c->d_count, c->stream));
     NS_CUDA(c, cudaMemcpyAsync(&h, c->d_count, sizeof h, cudaMemcpyDeviceToHost, c->stream));
     NS_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -657,7 +867,7 @@ int ns_time_kernels(ns_ctx *c, int iter0, int reps, double *ms, int *launches)
     for (int k = 0; k < NS_KC_COUNT; k++) launches[k] = 0;
     for (int q = 0; q < n; q++) launches[cls[q]]++;
     int rc = NS_OK;
-    if (c->src) {
+    if (c->src || c->sp.src) {
         cudaError_t e = ns::launch_set_iter(c->d_iter, iter0, c->stream);
         if (e != cudaSuccess) rc = cuda_err(c, e, "set iter");
     }

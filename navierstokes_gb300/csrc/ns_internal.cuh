@@ -62,6 +62,29 @@ struct StageCoef {
     int stage;
 };
 
+// Base flow seen by the split-precision stage (uniform in x, v = 0,
+// uniform p): per-row density and velocity, their FP64 DRP y-derivatives
+// rounded to FP32, and the constants.
+struct SplitMean {
+    const float *rho, *u, *drho, *du;
+    float p, gamma;
+};
+
+// Device state of the split-precision path (precision = NS_PREC_SPLIT).
+struct SplitState {
+    int fpitch = 0;                   // FP32 row pitch (elements)
+    float *q[2] = {nullptr, nullptr}; // perturbation ping-pong, 4 planes each
+    float *xc = nullptr, *yc = nullptr;
+    float *xcl = nullptr, *ycl = nullptr;  // FP64 table minus its FP32 rounding
+    float *sigx = nullptr, *sigy = nullptr, *src = nullptr;
+    float *rho_bc = nullptr;          // rhob(j) - rho_b(j)
+    float *ycorr = nullptr;           // [4][jmax]: y filter applied to Ub, minus Ub
+    float *mean_buf = nullptr;        // rho, u, drho, du: [4][jmax]
+    SplitMean mean{};
+    float p_bc = 0.f;                 // 1/gamma - p_b
+    int warm = 0, fx_chunks = 1, fy_chunks = 1;
+};
+
 }  // namespace ns
 
 struct ns_ctx {
@@ -89,6 +112,8 @@ struct ns_ctx {
     int warm = 0;       // filter warm-up length (-1: serial sweeps)
     int fx_chunks = 1, fy_chunks = 1;
     bool visc = false;
+    bool split = false;
+    ns::SplitState sp;
     bool have_state = false;
     // captured one-step graph
     cudaGraphExec_t step_exec = nullptr;
@@ -114,4 +139,8 @@ cudaError_t launch_count_nonfinite(const double *U, const Dims &d, unsigned long
 int count_step_launches(const ns_ctx *c);
 // Makes msg the text ns_last_error(NULL) returns (ns_api.cu).
 void record_error(const char *msg);
+// Split-precision path (ns_split.cu).
+cudaError_t launch_split_kernel(ns_ctx *c, int cls, int stage, cudaStream_t s);
+cudaError_t launch_split_from_full(ns_ctx *c, const double *U, cudaStream_t s);
+cudaError_t launch_split_to_full(ns_ctx *c, double *U, cudaStream_t s);
 }  // namespace ns

@@ -559,6 +559,7 @@ static cudaError_t launch_kernel_t(ns_ctx *c, int cls, int stage, cudaStream_t s
 
 cudaError_t launch_kernel(ns_ctx *c, int cls, int stage, cudaStream_t s)
 {
+    if (cls >= NS_KC_SPLIT_STAGE) return launch_split_kernel(c, cls, stage, s);
     if (c->visc)
         return c->d.nk == 5 ? launch_kernel_t<true, 5>(c, cls, stage, s)
                             : launch_kernel_t<true, 4>(c, cls, stage, s);
@@ -571,7 +572,16 @@ cudaError_t launch_kernel(ns_ctx *c, int cls, int stage, cudaStream_t s)
 int step_sequence(const ns_ctx *c, int *cls, int *stage)
 {
     int n = 0;
-    if (c->src) { cls[n] = NS_KC_STAGE_SIN; stage[n++] = 0; }
+    if (c->src || c->sp.src) { cls[n] = NS_KC_STAGE_SIN; stage[n++] = 0; }
+    if (c->split) {
+        for (int st = 0; st < 6; st++) {
+            cls[n] = NS_KC_SPLIT_STAGE; stage[n++] = st;
+            cls[n] = NS_KC_SPLIT_FX; stage[n++] = st;
+            cls[n] = NS_KC_SPLIT_FY; stage[n++] = st;
+            cls[n] = NS_KC_SPLIT_BC; stage[n++] = st;
+        }
+        return n;
+    }
     for (int st = 0; st < 6; st++) {
         if (c->visc) { cls[n] = NS_KC_PRIM; stage[n++] = st; }
         cls[n] = NS_KC_FIRST; stage[n++] = st;

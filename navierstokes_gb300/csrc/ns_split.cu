@@ -1,0 +1,601 @@
+// ns_split.cu -- split-precision stage loop: FP64 mean flow + FP32 perturbation.
+//
+// The state is U = Ub + q' with Ub the FP64 base flow (constant in time,
+// uniform in x, v = 0, p uniform) and q' = (rho',u',v',p') stored in FP32.
+// Every stencil and filter sum runs in FP32 over q'; the LDDRK accumulator w
+// (rk.f90:163) stays FP64.  The equations are the Euler right-hand side of
+// eqeuler.f90:53-92 (1/Re = 0) written for U = Ub + q': with dUb/dx = 0,
+// v_b = 0 and dp_b = 0 every term is perturbation-sized, so no FP32
+// difference of two O(1) numbers is ever formed.  The mean flow's own right
+// hand side vanishes; the y filter, whose REAL(4) boundary coefficients do
+// not preserve constants (filtering.f90:114-120), acts on Ub by a fixed
+// FP64 amount that is precomputed per row and added back.
+//
+// FP64 <-> FP32 conversions of the accumulator update are done with integer
+// bit operations (IEEE-754 layouts, round to nearest even): on GB300 the F2F
+// instructions run on the FP64 pipe, which is about 60x slower than FP32.
+#include "ns_internal.cuh"
+
+namespace ns {
+
+// ---------------------------------------------------------------------------
+// Exact conversions on the integer pipe
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double f2d_exact(float x)
+{
+    const unsigned b = __float_as_uint(x);
+    const unsigned e = (b >> 23) & 0xffu;
+    if (e == 0u || e == 0xffu) return (double)x;  // zero, subnormal, inf, nan
+    const unsigned m = b & 0x7fffffu;
+    const unsigned hi = (b & 0x80000000u) | ((e + (1023u - 127u)) << 20) | (m >> 3);
+    const unsigned lo = m << 29;
+    return __hiloint2double((int)hi, (int)lo);
+}
+
+__device__ __forceinline__ float d2f_rn(double x)
+{
+    const unsigned hi = (unsigned)__double2hiint(x);
+    const unsigned lo = (unsigned)__double2loint(x);
+    const unsigned e = (hi >> 20) & 0x7ffu;
+    // normal FP32 results only (exponent 2^-126 .. 2^127); the rest is rare
+    if (e < 1023u - 126u || e > 1023u + 127u) {
+        if (((hi & 0x7fffffffu) | lo) == 0u) return __uint_as_float(hi & 0x80000000u);
+        return (float)x;
+    }
+    const unsigned top = ((hi & 0xfffffu) << 3) | (lo >> 29);  // 23 mantissa bits
+    const unsigned rest = lo & 0x1fffffffu;                    // 29 discarded bits
+    unsigned f = (hi & 0x80000000u) | ((e - (1023u - 127u)) << 23) | top;
+    const unsigned half = 1u << 28;
+    if (rest > half || (rest == half && (top & 1u))) f += 1u;  // carry may bump the exponent
+    return __uint_as_float(f);
+}
+
+// ---------------------------------------------------------------------------
+// Fused stage kernel: FP32 derivatives from a shared-memory tile, Euler RHS,
+// FP64 LDDRK update, buffer damping.  Out of place (qin -> qout).
+// ---------------------------------------------------------------------------
+constexpr int kTX = 32, kTY = 16, kH = 3;
+constexpr int kSW = kTX + 2 * kH, kSH = kTY + 2 * kH;
+
+// One-sided closure, written as sum_z c_z*(f_z - f_q): the closure
+// coefficients sum to zero, and in this form a constant field gives exactly
+// zero in FP32 as well (their FP32 roundings no longer sum to zero).
+__device__ __forceinline__ float closure_f32(const float *__restrict__ g, long long st, int q,
+                                             int n, const float *__restrict__ c)
+{
+    const int o0 = (q < 3) ? -q : (n - 7 - q);
+    const float *p = g + (long long)o0 * st;
+    const float f0 = g[0];
+    float r = 0.f;
+#pragma unroll
+    for (int z = 0; z < 7; z++) r = fmaf(c[z], p[(long long)z * st] - f0, r);
+    return r;
+}
+
+// Float-float pieces (Knuth two-sum, FMA two-product) for the divergence.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
+{
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// sum_s c_s*(f[+s] - f[-s]) for s = 1..3 in float-float: the differences
+// exact (two-sum), each coefficient as hi + lo (the FP64 table value), the
+// products exact (FMA), the sum compensated.  Returns hi and lo.
+__device__ __forceinline__ void drp_ff(const float *fp, const float *fm, const float *ch,
+                                       const float *cl, float &hi, float &lo)
+{
+    hi = 0.f;
+    lo = 0.f;
+#pragma unroll
+    for (int s = 0; s < 3; s++) {
+        float dh, dl;
+        two_sum(fp[s], -fm[s], dh, dl);
+        const float ph = ch[s] * dh;
+        const float pl = fmaf(ch[s], dh, -ph) + fmaf(ch[s], dl, cl[s] * dh);
+        float sh, se;
+        two_sum(hi, ph, sh, se);
+        hi = sh;
+        lo += se + pl;
+    }
+}
+
+template <bool FIRST, bool SRC>
+__global__ void __launch_bounds__(256)
+    k_split_stage(Dims d, int fpitch, const float *__restrict__ qin, float *__restrict__ qout,
+                  double *__restrict__ W, const float *__restrict__ xc,
+                  const float *__restrict__ yc, const float *__restrict__ xcl,
+                  const float *__restrict__ ycl, const SplitMean mean,
+                  const float *__restrict__ sigx, const float *__restrict__ sigy,
+                  const float *__restrict__ src, const double *__restrict__ stage_sin,
+                  double dt, double alpha, double beta, int stage)
+{
+    __shared__ float sq[4][kSH][kSW];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int i0 = blockIdx.x * kTX, j0 = blockIdx.y * kTY;
+    const long long fplane = (long long)fpitch * d.jmax;
+    // cooperative tile load (halo 3; points outside the grid are never read)
+    for (int e = ty * kTX + tx; e < 4 * kSH * kSW; e += kTX * 8) {
+        const int k = e / (kSH * kSW);
+        const int r = (e / kSW) % kSH;
+        const int cidx = e % kSW;
+        const int gi = i0 - kH + cidx, gj = j0 - kH + r;
+        float v = 0.f;
+        if (gi >= 0 && gi < d.imax && gj >= 0 && gj < d.jmax)
+            v = qin[k * fplane + (long long)gj * fpitch + gi];
+        sq[k][r][cidx] = v;
+    }
+    __syncthreads();
+    const int i = i0 + tx;
+    if (i >= d.imax) return;
+    const float *cxp = xc + kCoefStride * i;
+    const float cx4 = cxp[4], cx5 = cxp[5], cx6 = cxp[6];
+    const bool xint = (i >= 3 && i < d.imax - 3);
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const int ly = ty + 8 * h;
+        const int j = j0 + ly;
+        if (j >= d.jmax) break;
+        const long long fidx = (long long)j * fpitch + i;
+        const long long didx = (long long)j * d.pitch + i;
+        const int sr = ly + kH, sc = tx + kH;
+        float q[4], gx[4], gy[4];
+        const float *cyp = yc + kCoefStride * j;
+        const bool yint = (j >= 3 && j < d.jmax - 3);
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            q[k] = sq[k][sr][sc];
+            if (xint) {
+                float r = cx4 * (sq[k][sr][sc + 1] - sq[k][sr][sc - 1]);
+                r = fmaf(cx5, sq[k][sr][sc + 2] - sq[k][sr][sc - 2], r);
+                gx[k] = fmaf(cx6, sq[k][sr][sc + 3] - sq[k][sr][sc - 3], r);
+            } else {
+                gx[k] = closure_f32(qin + k * fplane + fidx, 1, i, d.imax, cxp);
+            }
+            if (yint) {
+                float r = cyp[4] * (sq[k][sr + 1][sc] - sq[k][sr - 1][sc]);
+                r = fmaf(cyp[5], sq[k][sr + 2][sc] - sq[k][sr - 2][sc], r);
+                gy[k] = fmaf(cyp[6], sq[k][sr + 3][sc] - sq[k][sr - 3][sc], r);
+            } else {
+                gy[k] = closure_f32(qin + k * fplane + fidx, fpitch, j, d.jmax, cyp);
+            }
+        }
+        const bool interior = (i > 0) && (i < d.imax - 1) && (j > 0) && (j < d.jmax - 1);
+        if (interior) {
+            // Divergence du'/dx + dv'/dy, compensated where the interior
+            // stencil applies: for a nearly steady solenoidal field its two
+            // O(|u'|) terms cancel, and a plain FP32 rounding of them would
+            // be the same every stage and drive p' coherently.
+            float div;
+            if (xint && yint) {
+                const float fpx[3] = {sq[1][sr][sc + 1], sq[1][sr][sc + 2], sq[1][sr][sc + 3]};
+                const float fmx[3] = {sq[1][sr][sc - 1], sq[1][sr][sc - 2], sq[1][sr][sc - 3]};
+                const float fpy[3] = {sq[2][sr + 1][sc], sq[2][sr + 2][sc], sq[2][sr + 3][sc]};
+                const float fmy[3] = {sq[2][sr - 1][sc], sq[2][sr - 2][sc], sq[2][sr - 3][sc]};
+                const float chx[3] = {cx4, cx5, cx6}, clx[3] = {xcl[kCoefStride * i + 4],
+                                                                xcl[kCoefStride * i + 5],
+                                                                xcl[kCoefStride * i + 6]};
+                const float chy[3] = {cyp[4], cyp[5], cyp[6]},
+                            cly[3] = {ycl[kCoefStride * j + 4], ycl[kCoefStride * j + 5],
+                                      ycl[kCoefStride * j + 6]};
+                float xh, xl, yh, yl, sh, se;
+                drp_ff(fpx, fmx, chx, clx, xh, xl);
+                drp_ff(fpy, fmy, chy, cly, yh, yl);
+                two_sum(xh, yh, sh, se);
+                div = sh + (se + (xl + yl));
+            } else {
+                div = gx[1] + gy[2];
+            }
+            // U = Ub + q'; dUb/dx = 0, v_b = 0, dp_b = 0 (eqeuler.f90:63-92, 1/Re = 0)
+            const float rho = mean.rho[j] + q[0];
+            const float uu = mean.u[j] + q[1];
+            const float vv = q[2];
+            const float pp = mean.p + q[3];
+            const float rhoy = mean.drho[j] + gy[0];
+            const float uy = mean.du[j] + gy[1];
+            const float ri = 1.0f / rho;
+            float r[4];
+            // rho*du/dx + rho*dv/dy (eqeuler.f90:63) as rho*div
+            float t = uu * gx[0];
+            t = fmaf(vv, rhoy, t);
+            t = fmaf(rho, div, t);
+            r[0] = -t;
+            t = uu * gx[1];
+            t = fmaf(ri, gx[3], t);
+            t = fmaf(vv, uy, t);
+            r[1] = -t;
+            t = uu * gx[2];
+            t = fmaf(vv, gy[2], t);
+            t = fmaf(ri, gy[3], t);
+            r[2] = -t;
+            // gamma*p*du/dx + gamma*p*dv/dy (eqeuler.f90:80-82) as gamma*p*div
+            const float gp = mean.gamma * pp;
+            t = uu * gx[3];
+            t = fmaf(vv, gy[3], t);
+            t = fmaf(gp, div, t);
+            if (SRC) t = t - (float)stage_sin[stage] * src[fidx];
+            r[3] = -t;
+            // rk_steep (rk.f90:163-164): FP64 accumulator
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const double dr = f2d_exact((float)dt * r[k]);
+                const double w = FIRST ? dr : fma(alpha, W[k * d.plane + didx], dr);
+                W[k * d.plane + didx] = w;
+                q[k] = d2f_rn(fma(beta, w, f2d_exact(q[k])));
+            }
+        }
+        // bufferxy (rk.f90:77-151): U - Ub = q'
+        if (j < d.D || j >= d.jmax - d.D) {
+            const float s = sigy[j];
+#pragma unroll
+            for (int k = 0; k < 4; k++) q[k] *= s;
+        }
+        if (i < d.D || i >= d.imax - d.D) {
+            const float s = sigx[i];
+#pragma unroll
+            for (int k = 0; k < 4; k++) q[k] *= s;
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++) qout[k * fplane + fidx] = q[k];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// FP32 filter recurrences (filtering.f90) over q'.  Same three passes and
+// chunking as the FP64 kernel (ns_kernels.cu); here one warp stages its 32
+// lines through shared memory so that every global access is coalesced.
+// ---------------------------------------------------------------------------
+// Filter coefficients for the FP32 sweeps, in forms that keep a constant
+// field exactly constant: the 13-point filter as
+//   v = u0 + sum_s m_s*((u_s - u0) + (u_-s - u0)),  m_s = -sigmaf*df(s)
+// (its coefficients sum to 0 up to 3e-17, which is dropped), and the
+// boundary filter as
+//   v = u0 + sum_{s != 0} b_s*(u_s - u0) + bsum*u0,  bsum = -sigmaf*sum(dfb)
+// with bsum the FP64 sum, which carries the reference's REAL(4) coefficient
+// sum in y (-8.4e-9) and is ~1e-17 in x.  Rounding the coefficients to FP32
+// then changes the filter's response only at nonzero wavenumbers; with the
+// plain forms every application scaled the smooth part of q' by 1 + 3e-8.
+struct FiltF {
+    float m[7];      // m[s], s = 1..6
+    float bm1, b[6]; // b(-1), b[s] s = 1..5
+    float bsum;
+};
+
+// The second differences are formed as (u_s - u0) + (u_-s - u0): for a
+// smooth field the two differences are exact (Sterbenz) and small, so the
+// rounding is relative to the second difference, not to |u|; summing
+// u_s + u_-s first would round at |u|*6e-8, the same pattern every
+// application for a steady structure such as a vortex.
+__device__ __forceinline__ float pass2_f(const float *w, const FiltF &f)
+{
+    const float u0 = w[6];
+    float acc = f.m[6] * ((w[12] - u0) + (w[0] - u0));
+    acc = fmaf(f.m[5], (w[11] - u0) + (w[1] - u0), acc);
+    acc = fmaf(f.m[4], (w[10] - u0) + (w[2] - u0), acc);
+    acc = fmaf(f.m[3], (w[9] - u0) + (w[3] - u0), acc);
+    acc = fmaf(f.m[2], (w[8] - u0) + (w[4] - u0), acc);
+    acc = fmaf(f.m[1], w[7] - u0, acc);
+    return fmaf(f.m[1], w[5] - u0, u0 + acc);
+}
+
+// Boundary filter at window position p: neighbours p-1 (newest) and
+// p+1..p+5 (pass 1), or mirrored (pass 3, dir = -1).
+template <int DIR>
+__device__ __forceinline__ float passb_f(const float *w, int p, const FiltF &f)
+{
+    const float u0 = w[p];
+    float acc = f.bsum * u0;
+#pragma unroll
+    for (int z = 1; z <= 5; z++) acc = fmaf(f.b[z], w[p + DIR * z] - u0, acc);
+    return fmaf(f.bm1, w[p - DIR] - u0, u0 + acc);
+}
+
+// y filter: thread per (column, variable, chunk); lanes on consecutive
+// columns, so each step reads and writes one coalesced row segment.
+// corr[k*jmax + j] is the FP64 action of the filter on the base flow.
+__global__ void __launch_bounds__(128)
+    k_split_filter_y(Dims d, int fpitch, const float *__restrict__ src, float *__restrict__ dst,
+                     int chunks, int warm, FiltF f, const float *__restrict__ corr)
+{
+    const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long total = (long long)d.imax * 4 * chunks;
+    if (gid >= total) return;
+    const int line = (int)(gid % d.imax);
+    const int rest = (int)(gid / d.imax);
+    const int k = rest % 4, c = rest / 4;
+    const int n = d.jmax;
+    const long long st = fpitch;
+    const long long base = (long long)k * fpitch * d.jmax + line;
+    const float *__restrict__ s = src + base;
+    float *__restrict__ o = dst + base;
+    const float *__restrict__ cr = corr + (long long)k * d.jmax;
+    const int len2 = n - 12;
+    const int a = 6 + (int)(((long long)c * len2) / chunks);
+    const int b = 6 + (int)(((long long)(c + 1) * len2) / chunks);
+    float w[13];
+    int q;
+    if (c == 0 || warm < 0 || a - warm <= 6) {
+#pragma unroll
+        for (int t = 0; t < 13; t++) w[t] = s[t * st];
+#pragma unroll
+        for (int p = 1; p <= 6; p++) w[p] = passb_f<1>(w, p, f);
+        if (c == 0) {
+#pragma unroll
+            for (int p = 0; p < 6; p++) o[p * st] = w[p] + cr[p];
+        }
+        q = 6;
+    } else {
+        q = a - warm;
+#pragma unroll
+        for (int t = 0; t < 13; t++) w[t] = s[(long long)(q - 6 + t) * st];
+    }
+    for (; q < b; q++) {
+        const float v = pass2_f(w, f);
+        if (q >= a) o[(long long)q * st] = v + cr[q];
+#pragma unroll
+        for (int t = 0; t < 5; t++) w[t] = w[t + 1];
+        w[5] = v;
+#pragma unroll
+        for (int t = 6; t < 12; t++) w[t] = w[t + 1];
+        w[12] = (q + 7 < n) ? s[(long long)(q + 7) * st] : 0.f;
+    }
+    if (c == chunks - 1) {
+#pragma unroll
+        for (int x = 10; x >= 5; x--) w[x] = passb_f<-1>(w, x, f);
+#pragma unroll
+        for (int x = 5; x < 12; x++) o[(long long)(n - 12 + x) * st] = w[x] + cr[n - 12 + x];
+    }
+}
+
+// x filter: each warp owns 32 consecutive rows of one variable and one
+// chunk.  The old values a lane appends to its window (position q+7 at step
+// q) are staged 32 positions at a time through a [32][33] tile loaded with
+// coalesced row reads; the outputs go back the same way.
+constexpr int kXW = 4;  // warps per block
+
+__global__ void __launch_bounds__(32 * kXW)
+    k_split_filter_x(Dims d, int fpitch, const float *__restrict__ src, float *__restrict__ dst,
+                     int chunks, int warm, FiltF f)
+{
+    __shared__ float tin[kXW][32][33];
+    __shared__ float tout[kXW][32][33];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int rows32 = (d.jmax + 31) / 32;
+    const long long gw = (long long)blockIdx.x * kXW + wid;  // global warp
+    const long long nw = (long long)rows32 * 4 * chunks;
+    if (gw >= nw) return;                                       // whole warp exits together
+    const int rg = (int)(gw % rows32);
+    const int rest = (int)(gw / rows32);
+    const int k = rest % 4, c = rest / 4;
+    const int n = d.imax;
+    const int row0 = rg * 32;
+    const int nrows = min(32, d.jmax - row0);
+    const long long fplane = (long long)fpitch * d.jmax;
+    const float *__restrict__ sbase = src + k * fplane + (long long)row0 * fpitch;
+    float *__restrict__ obase = dst + k * fplane + (long long)row0 * fpitch;
+    const bool active = lane < nrows;
+    const float *__restrict__ s = sbase + (long long)(active ? lane : 0) * fpitch;
+    float(*ti)[33] = tin[wid];
+    float(*to)[33] = tout[wid];
+
+    const int len2 = n - 12;
+    const int a = 6 + (int)(((long long)c * len2) / chunks);
+    const int b = 6 + (int)(((long long)(c + 1) * len2) / chunks);
+    const bool exact = (c == 0 || warm < 0 || a - warm <= 6);
+    const int q0 = exact ? 6 : a - warm;
+
+    float w[13];
+    if (exact) {
+#pragma unroll
+        for (int t = 0; t < 13; t++) w[t] = s[t];
+#pragma unroll
+        for (int p = 1; p <= 6; p++) w[p] = passb_f<1>(w, p, f);
+        if (c == 0 && active)
+            for (int p = 0; p < 6; p++) obase[(long long)lane * fpitch + p] = w[p];
+    } else {
+#pragma unroll
+        for (int t = 0; t < 13; t++) w[t] = s[q0 - 6 + t];
+    }
+    // Steps q = q0 .. b-1 in blocks of 32: block B covers steps
+    // [q0+32B, q0+32B+32), appends positions q+7, writes outputs at q.
+    for (int qb = q0; qb < b; qb += 32) {
+        const int pin = qb + 7;  // first appended position of the block
+        // stage appended positions pin .. pin+31 (clipped to n)
+        for (int r = 0; r < nrows; r++) {
+            const int pos = pin + lane;
+            ti[r][lane] = (pos < n) ? sbase[(long long)r * fpitch + pos] : 0.f;
+        }
+        __syncwarp();
+        const int nstep = min(32, b - qb);
+        for (int t = 0; t < nstep; t++) {
+            const float v = pass2_f(w, f);
+            to[lane][t] = v;
+#pragma unroll
+            for (int u = 0; u < 5; u++) w[u] = w[u + 1];
+            w[5] = v;
+#pragma unroll
+            for (int u = 6; u < 12; u++) w[u] = w[u + 1];
+            w[12] = ti[lane][t];
+        }
+        __syncwarp();
+        // write outputs q = qb .. qb+nstep-1 that this chunk owns (q >= a)
+        for (int r = 0; r < nrows; r++) {
+            const int qq = qb + lane;
+            if (lane < nstep && qq >= a) obase[(long long)r * fpitch + qq] = to[r][lane];
+        }
+        __syncwarp();
+    }
+    if (c == chunks - 1 && active) {
+        // w[0..11] = positions n-12 .. n-1 (pass 3)
+#pragma unroll
+        for (int x = 10; x >= 5; x--) w[x] = passb_f<-1>(w, x, f);
+        for (int x = 5; x < 12; x++) obase[(long long)lane * fpitch + (n - 12 + x)] = w[x];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// ccpml (cc.f90:6-68) on q': rho'(1,j) = rhob(j) - rho_b(j), v' = 0,
+// p' = 1/gamma - p_b on every edge; extrapolations are the same in q'.
+// ---------------------------------------------------------------------------
+__global__ void k_split_bc(Dims d, int fpitch, float *__restrict__ q,
+                           const float *__restrict__ rho_bc, float p_bc)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const long long P = (long long)fpitch * d.jmax;
+    auto colval = [&](int i, int j, float *v) {
+        const long long r = (long long)j * fpitch;
+        if (i == 0) {
+            v[0] = rho_bc[j];
+            v[1] = 2.f * q[P + r + 1] - q[P + r + 2];
+            v[2] = 0.f;
+            v[3] = p_bc;
+        } else {
+            const int a = d.imax - 2, b = d.imax - 3;
+            for (int k = 0; k < 3; k++) v[k] = 2.f * q[k * P + r + a] - q[k * P + r + b];
+            v[3] = p_bc;
+        }
+    };
+    float v[4];
+    if (t > 0 && t < d.jmax - 1) {
+        const long long r = (long long)t * fpitch;
+        colval(0, t, v);
+        for (int k = 0; k < 4; k++) q[k * P + r] = v[k];
+        colval(d.imax - 1, t, v);
+        for (int k = 0; k < 4; k++) q[k * P + r + d.imax - 1] = v[k];
+    }
+    if (t < d.imax) {
+        const int jt = d.jmax - 1;
+        float a[4], b[4];
+        if (t == 0 || t == d.imax - 1) {
+            colval(t, jt - 1, a);
+            colval(t, jt - 2, b);
+        } else {
+            for (int k = 0; k < 4; k++) {
+                a[k] = q[k * P + (long long)(jt - 1) * fpitch + t];
+                b[k] = q[k * P + (long long)(jt - 2) * fpitch + t];
+            }
+        }
+        for (int k = 0; k < 3; k++) q[k * P + (long long)jt * fpitch + t] = 2.f * a[k] - b[k];
+        q[3 * P + (long long)jt * fpitch + t] = p_bc;
+        if (t == 0 || t == d.imax - 1) {
+            colval(t, 1, a);
+            colval(t, 2, b);
+        } else {
+            for (int k = 0; k < 4; k++) {
+                a[k] = q[k * P + (long long)1 * fpitch + t];
+                b[k] = q[k * P + (long long)2 * fpitch + t];
+            }
+        }
+        for (int k = 0; k < 3; k++) q[k * P + t] = 2.f * a[k] - b[k];
+        q[3 * P + t] = p_bc;
+    }
+}
+
+// State conversion: q' = f32(U - Ub) and U = Ub + q'.
+__global__ void k_split_from_full(Dims d, int fpitch, const double *__restrict__ U,
+                                  const double *__restrict__ Ub, float *__restrict__ q)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= d.imax || j >= d.jmax) return;
+    for (int k = 0; k < 4; k++) {
+        const long long di = k * d.plane + (long long)j * d.pitch + i;
+        q[(long long)k * fpitch * d.jmax + (long long)j * fpitch + i] = (float)(U[di] - Ub[di]);
+    }
+}
+
+__global__ void k_split_to_full(Dims d, int fpitch, const float *__restrict__ q,
+                                const double *__restrict__ Ub, double *__restrict__ U)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= d.imax || j >= d.jmax) return;
+    for (int k = 0; k < 4; k++) {
+        const long long di = k * d.plane + (long long)j * d.pitch + i;
+        U[di] = Ub[di] + (double)q[(long long)k * fpitch * d.jmax + (long long)j * fpitch + i];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------
+static FiltF to_f32(const FilterCoef &c)
+{
+    // FilterCoef holds m[s] = -sigmaf*df(s), bm1 = -sigmaf*dfb(-1),
+    // b[s] = -sigmaf*dfb(s) and b0 = 1 - sigmaf*dfb(0) (ns_api.cu)
+    FiltF f;
+    for (int s = 0; s < 7; s++) f.m[s] = (float)c.m[s];
+    f.bm1 = (float)c.bm1;
+    double sum = c.bm1 + (c.b0 - 1.0);
+    for (int s = 0; s < 6; s++) {
+        f.b[s] = (float)c.b[s];
+        if (s >= 1) sum += c.b[s];
+    }
+    f.bsum = (float)sum;
+    return f;
+}
+
+cudaError_t launch_split_kernel(ns_ctx *c, int cls, int stage, cudaStream_t s)
+{
+    const Dims &d = c->d;
+    SplitState &sp = c->sp;
+    // buffer roles alternate every stage; a step has six stages, so the
+    // roles at the start of every step are the same
+    float *qa = sp.q[stage & 1], *qb = sp.q[(stage + 1) & 1];
+    switch (cls) {
+    case NS_KC_SPLIT_STAGE: {
+        const dim3 blk(kTX, 8), grd((d.imax + kTX - 1) / kTX, (d.jmax + kTY - 1) / kTY);
+        const bool src = sp.src != nullptr;
+#define NS_SPL(FIRST, SRC)                                                                      \
+    k_split_stage<FIRST, SRC><<<grd, blk, 0, s>>>(d, sp.fpitch, qa, qb, c->W, sp.xc, sp.yc,    \
+                                                  sp.xcl, sp.ycl, sp.mean, sp.sigx, sp.sigy,   \
+                                                  sp.src,                                      \
+                                                  c->stage_sin, c->p.dt, c->alpha[stage],      \
+                                                  c->beta[stage], stage)
+        if (stage == 0) {
+            if (src) NS_SPL(true, true); else NS_SPL(true, false);
+        } else {
+            if (src) NS_SPL(false, true); else NS_SPL(false, false);
+        }
+#undef NS_SPL
+        break;
+    }
+    case NS_KC_SPLIT_FX: {
+        const long long warps = (long long)((d.jmax + 31) / 32) * 4 * sp.fx_chunks;
+        k_split_filter_x<<<(unsigned)((warps + kXW - 1) / kXW), 32 * kXW, 0, s>>>(
+            d, sp.fpitch, qb, qa, sp.fx_chunks, sp.warm, to_f32(c->fx));
+        break;
+    }
+    case NS_KC_SPLIT_FY: {
+        const long long t = (long long)d.imax * 4 * sp.fy_chunks;
+        k_split_filter_y<<<(unsigned)((t + 127) / 128), 128, 0, s>>>(
+            d, sp.fpitch, qa, qb, sp.fy_chunks, sp.warm, to_f32(c->fy), sp.ycorr);
+        break;
+    }
+    case NS_KC_SPLIT_BC: {
+        const int nt = d.imax > d.jmax ? d.imax : d.jmax;
+        k_split_bc<<<(nt + 127) / 128, 128, 0, s>>>(d, sp.fpitch, qb, sp.rho_bc, sp.p_bc);
+        break;
+    }
+    default:
+        return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_split_from_full(ns_ctx *c, const double *U, cudaStream_t s)
+{
+    const dim3 blk(32, 8), grd((c->d.imax + 31) / 32, (c->d.jmax + 7) / 8);
+    k_split_from_full<<<grd, blk, 0, s>>>(c->d, c->sp.fpitch, U, c->Ubase, c->sp.q[0]);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_split_to_full(ns_ctx *c, double *U, cudaStream_t s)
+{
+    const dim3 blk(32, 8), grd((c->d.imax + 31) / 32, (c->d.jmax + 7) / 8);
+    k_split_to_full<<<grd, blk, 0, s>>>(c->d, c->sp.fpitch, c->sp.q[0], c->Ubase, U);
+    return cudaGetLastError();
+}
+
+}  // namespace ns

@@ -1,0 +1,130 @@
+"""Split precision (FP64 base flow + FP32 perturbation) against the plain
+FP64 path on the GPU, measured on the pressure perturbation p' = p - p_b.
+
+Acoustic cases (pulse, source, sheared base flow): relative L2 and max error
+<= 1e-5 against the FP64 run.  With a perturbation ten times larger than the
+acoustic one in the field (the 1e-3 vortex beside the 1e-4 pulse), the FP32
+state cannot resolve changes below half an ulp of that vortex (6e-11 at
+|u'| = 1e-3) that the FP64 run makes (the filter trimming its high
+wavenumbers): p' then carries an offset of about ten such ulps next to the
+vortex.  The bound there is 50 FP32 ulps of the largest perturbation."""
+import numpy as np
+import pytest
+
+from navierstokes_gb300 import _lib as L
+from navierstokes_gb300 import cases
+
+pytestmark = pytest.mark.gpu
+TOL_PPRIME = 1e-5
+
+
+def p_errors(split, ref, base):
+    dp = split[..., 3] - ref[..., 3]
+    pr = ref[..., 3] - base[..., 3]
+    l2 = float(np.linalg.norm(dp) / np.linalg.norm(pr))
+    mx = float(np.max(np.abs(dp)) / np.max(np.abs(pr)))
+    return l2, mx
+
+
+def run(case, nsteps, precision, iter0=0):
+    from navierstokes_gb300 import Solver
+    with Solver(case, precision=precision) as s:
+        return s.run(case.U0, iter0, nsteps)
+
+
+@pytest.mark.parametrize("mach", [0.0, 0.5])
+def test_split_matches_fp64_pulse(nslib, mach):
+    c = cases.uniform_flow_case(imax=600, jmax=480, mach=mach, vortex_eps=0.0, steps=300)
+    ref = run(c, 300, L.NS_PREC_FP64)
+    got = run(c, 300, L.NS_PREC_SPLIT)
+    l2, mx = p_errors(got, ref, c.Ub)
+    print(f"pulse, mach {mach}: p' rel L2 {l2:.2e} max {mx:.2e}")
+    assert l2 <= TOL_PPRIME and mx <= TOL_PPRIME
+
+
+@pytest.mark.parametrize("mach", [0.0, 0.5])
+def test_split_pulse_and_vortex_within_fp32_floor(nslib, mach):
+    c = cases.uniform_flow_case(imax=600, jmax=480, mach=mach, vortex_upstream=100, steps=300)
+    ref = run(c, 300, L.NS_PREC_FP64)
+    got = run(c, 300, L.NS_PREC_SPLIT)
+    l2, mx = p_errors(got, ref, c.Ub)
+    print(f"pulse+vortex, mach {mach}: p' rel L2 {l2:.2e} max {mx:.2e}")
+    qmax = max(np.max(np.abs(c.U0[..., k] - c.Ub[..., k])) for k in range(4))
+    ulp = 2.0 ** -24 * qmax
+    # rho', p': within 50 FP32 ulps of the largest perturbation
+    for k in (0, 3):
+        assert np.max(np.abs(got[..., k] - ref[..., k])) <= 50 * ulp
+    # u', v' of the (nearly steady) vortex keep the FP32 value when the FP64
+    # run changes them by less than half an ulp per update: a slow drift,
+    # bounded here by 500 ulps over 300 steps
+    for k in (1, 2):
+        assert np.max(np.abs(got[..., k] - ref[..., k])) <= 500 * ulp
+    assert l2 <= 1e-4
+
+
+def test_split_with_source_and_chunked_filters(nslib):
+    c = cases.uniform_flow_case(imax=1500, jmax=1100, mach=0.3, pulse_amp=0.0, vortex_eps=0.0,
+                                steps=80)
+    c.source_mode = L.NS_SRC_GAUSSIAN
+    c.amplitude, c.wf, c.m_pt, c.n_pt, c.r0 = 1e-3, 0.6, 0.0, 0.0, 3.0
+    ref = run(c, 80, L.NS_PREC_FP64, iter0=5)
+    got = run(c, 80, L.NS_PREC_SPLIT, iter0=5)
+    l2, mx = p_errors(got, ref, c.Ub)
+    print(f"source: p' rel L2 {l2:.2e} max {mx:.2e}")
+    assert l2 <= TOL_PPRIME and mx <= TOL_PPRIME
+
+
+def test_split_uniform_state_drift_matches_fp64(nslib):
+    """The REAL(4) y boundary filter moves a uniform state (its coefficients
+    sum to -8.4e-9); the split path adds that FP64 action on the base flow
+    back, so its drift matches the FP64 path's."""
+    c = cases.uniform_flow_case(imax=300, jmax=260, pulse_amp=0.0, vortex_eps=0.0)
+    c.U0 = c.Ub.copy()
+    ref = run(c, 20, L.NS_PREC_FP64)
+    got = run(c, 20, L.NS_PREC_SPLIT)
+    drift = np.max(np.abs(ref - c.Ub))
+    assert drift > 1e-9
+    assert np.max(np.abs(got - ref)) <= 1e-3 * drift
+
+
+def test_split_rk_euler_and_probes(nslib):
+    from navierstokes_gb300 import Solver
+    c = cases.uniform_flow_case(imax=128, jmax=96, vortex_upstream=30, steps=5)
+    U = c.U0.copy()
+    with Solver(c, precision=L.NS_PREC_SPLIT) as s:
+        for it in range(3):
+            s.rk_euler(U, 0.0, it)
+        res = s.run(c.U0, 0, 3)
+        pr = s.probes([64], [48])
+    # the host round trip U = Ub + q' -> q' = f32(U - Ub) loses the low bits
+    # of tiny q' (below 2^-52 |Ub|) at every call; the two paths agree to
+    # well below the FP32 resolution of the perturbation
+    print("rk_euler vs resident max diff", np.max(np.abs(U - res)))
+    np.testing.assert_allclose(U, res, rtol=0, atol=1e-11)
+    np.testing.assert_array_equal(pr[0], res[47, 63])
+
+
+def test_split_sheared_mean_flow(nslib):
+    """A base flow that varies in y (the reference's mixing layer, Euler,
+    with its acoustic source): the y-derivatives of the base flow enter the
+    perturbation equations as FP64-computed per-row terms."""
+    c = cases.mixing_layer_case(imax=200, jmax=160, nk=4, D=24)
+    c.inviscid = True
+    ref = run(c, 40, L.NS_PREC_FP64)
+    got = run(c, 40, L.NS_PREC_SPLIT)
+    l2, mx = p_errors(got, ref, c.Ub)
+    print(f"mixing layer: p' rel L2 {l2:.2e} max {mx:.2e}")
+    assert l2 <= TOL_PPRIME and mx <= TOL_PPRIME
+
+
+def test_split_rejects_unsupported(nslib):
+    from navierstokes_gb300 import Solver
+    c = cases.stretched_ns_case(imax=64, jmax=48, D=8, vortex_upstream=10)
+    with pytest.raises(L.NsError) as e:
+        Solver(c, precision=L.NS_PREC_SPLIT)          # Navier-Stokes
+    assert e.value.code == L.NS_ERR_UNSUPPORTED
+    u = cases.uniform_flow_case(imax=64, jmax=48, D=8, vortex_upstream=10)
+    u.Ub[:, :, 2] = 1e-3                              # base flow with v != 0
+    with pytest.raises(L.NsError) as e:
+        Solver(u, precision=L.NS_PREC_SPLIT)
+    assert e.value.code == L.NS_ERR_UNSUPPORTED
