@@ -203,6 +203,96 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+# Algorithmic HBM bytes per point of one launch of the split-precision
+# kernels (nk = 4): stage reads q' (4 x FP32) and w (4 x FP64) and writes
+# both; each filter reads and writes q'.
+SPLIT_BYTES_PER_POINT = {"k_split_stage": 96, "k_split_filter_x": 32,
+                         "k_split_filter_y": 32}
+SPLIT_STEP_BYTES_MIN = 960   # per point-step: 6 x (96 + 2 x 32)
+
+
+def split_study(args, local, hbm_peak):
+    """Config-3 workload: Euler, 4096x4096 uniform grid, M = 0.5, pulse 1e-4,
+    vortex 1e-3, 1000 steps; split precision against plain FP64 (throughput
+    of both and p' = p - p_b error at steps 100/500/1000)."""
+    import ctypes as C
+    import torch
+    from navierstokes_gb300 import Solver, cases
+    from navierstokes_gb300 import _lib as L
+    case = cases.uniform_flow_case(imax=args.split_n, jmax=args.split_n)
+    out = {"workload": f"Euler {case.imax}x{case.jmax} uniform grid, M=0.5, pulse 1e-4, "
+                       f"isentropic vortex 1e-3, D=30, sigma_f=0.2, CFL 0.5, dt={case.dt:.3g}",
+           "error_steps": args.split_error_steps}
+    stream = torch.cuda.Stream()
+    rates = {}
+    states = {}
+    kernels = {}
+    for name, prec in (("fp64", L.NS_PREC_FP64), ("split", L.NS_PREC_SPLIT)):
+        s = Solver(case, device=local, precision=prec)
+        s.set_stream(stream.cuda_stream)
+        s.set_state(case.U0)
+        done = 0
+        snaps = {}
+        for n in args.split_error_steps:
+            s.step(done, n - done)
+            done = n
+            snaps[n] = s.get_state()
+        states[name] = snaps
+        for it in range(args.warmup):
+            s.step(done + it, 1)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for k in range(args.steps):
+            s.step(done + args.warmup + k, 1)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        rates[name] = {"value": case.points / (ms * 1e-3) / 1e6, "ms_per_step": ms,
+                       "gpu_launches_per_step": s.launches_per_step()}
+        if name == "split":
+            kms = (C.c_double * L.NS_KC_COUNT)()
+            kn = (C.c_int * L.NS_KC_COUNT)()
+            L.check(s.lib.ns_time_kernels(s._ctx, 20_000, 2, kms, kn), s._ctx)
+            for k in range(L.NS_KC_COUNT):
+                if kn[k]:
+                    kname = s.lib.ns_kernel_name(k).decode()
+                    bpp = SPLIT_BYTES_PER_POINT.get(kname)
+                    kernels[kname] = {"ms_per_launch": kms[k], "launches_per_step": kn[k]}
+                    if bpp:
+                        gbs = bpp * case.points / (kms[k] * 1e-3) / 1e9
+                        kernels[kname]["achieved_gbs"] = gbs
+                        kernels[kname]["hbm_frac"] = gbs / hbm_peak
+        s.close()
+    tot = sum(v["ms_per_launch"] * v["launches_per_step"] for v in kernels.values())
+    for v in kernels.values():
+        v["share"] = v["ms_per_launch"] * v["launches_per_step"] / tot
+    dom = max(kernels, key=lambda n: kernels[n]["share"])
+    errs = {}
+    for n in args.split_error_steps:
+        a, b = states["fp64"][n], states["split"][n]
+        dp = b[..., 3] - a[..., 3]
+        pr = a[..., 3] - case.Ub[..., 3]
+        errs[str(n)] = {"p_rel_l2": float(np.linalg.norm(dp) / np.linalg.norm(pr)),
+                        "p_rel_max": float(np.max(np.abs(dp)) / np.max(np.abs(pr))),
+                        "p_abs_max": float(np.max(np.abs(dp)))}
+    step_gbs = SPLIT_STEP_BYTES_MIN * case.points / (rates["split"]["ms_per_step"] * 1e-3) / 1e9
+    out.update({"value": rates["split"]["value"], "unit": UNIT,
+                "fp64_value": rates["fp64"]["value"],
+                "speedup_vs_fp64": rates["split"]["value"] / rates["fp64"]["value"],
+                "ms_per_step": rates["split"]["ms_per_step"],
+                "fp64_ms_per_step": rates["fp64"]["ms_per_step"],
+                "p_error_vs_fp64": errs,
+                "roofline": {"bound": "hbm", "kernel": dom,
+                             "achieved": kernels[dom].get("achieved_gbs"),
+                             "peak": hbm_peak, "unit": "GB/s",
+                             "frac": kernels[dom].get("hbm_frac"),
+                             "step_frac_of_960B_per_point": step_gbs / hbm_peak},
+                "kernels": kernels})
+    return out
+
+
 def cpu_baseline_sample(case, seconds=20.0):
     """Oracle on the host cores, a bounded sample of the same workload."""
     import oracle
@@ -336,6 +426,13 @@ def run_ours(args, world, rank, local, pg):
     e2e_val = world * case.points * args.steps / t_e2e / 1e6
     nbytes = case.state_bytes()
 
+    split = None
+    if rank == 0 and world == 1 and not args.no_split:
+        try:
+            split = split_study(args, local, hbm_peak)
+        except Exception as e:
+            split = {"failed": str(e)}
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
@@ -359,6 +456,8 @@ def run_ours(args, world, rank, local, pg):
                 "roofline": roof, "kernels": kernels, "clocks": clocks}
         if cpu is not None:
             line["cpu_baseline"] = cpu
+        if split is not None:
+            line["split_precision"] = split
         print(json.dumps(line), flush=True)
 
 
@@ -372,6 +471,11 @@ def main():
     ap.add_argument("--jmax", type=int, default=2048)
     ap.add_argument("--nk", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-split", action="store_true",
+                    help="skip the split-precision (config-3) study")
+    ap.add_argument("--split-n", type=int, default=4096)
+    ap.add_argument("--split-error-steps", type=lambda t: [int(x) for x in t.split(",")],
+                    default=[100, 500, 1000])
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -893,8 +893,10 @@ int ns_time_kernels(ns_ctx *c, int iter0, int reps, double *ms, int *launches)
 
 const char *ns_kernel_name(int k)
 {
-    static const char *names[NS_KC_COUNT] = {"k_stage_sin", "k_prim",     "k_first", "k_update",
-                                             "k_filter_x",  "k_filter_y", "k_bc"};
+    static const char *names[NS_KC_COUNT] = {
+        "k_stage_sin",   "k_prim",          "k_first",          "k_update",
+        "k_filter_x",    "k_filter_y",      "k_bc",             "k_split_stage",
+        "k_split_filter_x", "k_split_filter_y", "k_split_bc"};
     return (k >= 0 && k < NS_KC_COUNT) ? names[k] : "";
 }
 

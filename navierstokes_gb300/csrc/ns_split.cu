@@ -25,7 +25,8 @@ __device__ __forceinline__ double f2d_exact(float x)
 {
     const unsigned b = __float_as_uint(x);
     const unsigned e = (b >> 23) & 0xffu;
-    if (e == 0u || e == 0xffu) return (double)x;  // zero, subnormal, inf, nan
+    if ((b & 0x7fffffffu) == 0u) return __hiloint2double((int)(b & 0x80000000u), 0);  // +-0
+    if (e == 0u || e == 0xffu) return (double)x;  // subnormal, inf, nan
     const unsigned m = b & 0x7fffffu;
     const unsigned hi = (b & 0x80000000u) | ((e + (1023u - 127u)) << 20) | (m >> 3);
     const unsigned lo = m << 29;
@@ -109,22 +110,36 @@ __global__ void __launch_bounds__(256)
                   const float *__restrict__ ycl, const SplitMean mean,
                   const float *__restrict__ sigx, const float *__restrict__ sigy,
                   const float *__restrict__ src, const double *__restrict__ stage_sin,
-                  double dt, double alpha, double beta, int stage)
+                  float dt, double alpha, double beta, int stage)
 {
     __shared__ float sq[4][kSH][kSW];
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int i0 = blockIdx.x * kTX, j0 = blockIdx.y * kTY;
     const long long fplane = (long long)fpitch * d.jmax;
+    // the FP64 accumulators of this thread's two points, requested before
+    // the tile so that their latency overlaps the tile load
+    double wold[2][4];
+    if (!FIRST) {
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int j = j0 + ty + 8 * h, i = i0 + tx;
+            const bool ok = i < d.imax && j < d.jmax;
+            const long long didx = (long long)j * d.pitch + i;
+#pragma unroll
+            for (int k = 0; k < 4; k++) wold[h][k] = ok ? W[k * d.plane + didx] : 0.0;
+        }
+    }
     // cooperative tile load (halo 3; points outside the grid are never read)
-    for (int e = ty * kTX + tx; e < 4 * kSH * kSW; e += kTX * 8) {
-        const int k = e / (kSH * kSW);
-        const int r = (e / kSW) % kSH;
-        const int cidx = e % kSW;
-        const int gi = i0 - kH + cidx, gj = j0 - kH + r;
-        float v = 0.f;
-        if (gi >= 0 && gi < d.imax && gj >= 0 && gj < d.jmax)
-            v = qin[k * fplane + (long long)gj * fpitch + gi];
-        sq[k][r][cidx] = v;
+    for (int r = ty; r < kSH; r += 8) {
+        const int gj = j0 - kH + r;
+        const bool rowok = gj >= 0 && gj < d.jmax;
+        for (int cc = tx; cc < kSW; cc += kTX) {
+            const int gi = i0 - kH + cc;
+            const bool ok = rowok && gi >= 0 && gi < d.imax;
+            const long long g = (long long)gj * fpitch + gi;
+#pragma unroll
+            for (int k = 0; k < 4; k++) sq[k][r][cc] = ok ? qin[k * fplane + g] : 0.f;
+        }
     }
     __syncthreads();
     const int i = i0 + tx;
@@ -219,8 +234,8 @@ __global__ void __launch_bounds__(256)
             // rk_steep (rk.f90:163-164): FP64 accumulator
 #pragma unroll
             for (int k = 0; k < 4; k++) {
-                const double dr = f2d_exact((float)dt * r[k]);
-                const double w = FIRST ? dr : fma(alpha, W[k * d.plane + didx], dr);
+                const double dr = f2d_exact(dt * r[k]);
+                const double w = FIRST ? dr : fma(alpha, wold[h][k], dr);
                 W[k * d.plane + didx] = w;
                 q[k] = d2f_rn(fma(beta, w, f2d_exact(q[k])));
             }
@@ -330,14 +345,34 @@ __global__ void __launch_bounds__(128)
 #pragma unroll
         for (int t = 0; t < 13; t++) w[t] = s[(long long)(q - 6 + t) * st];
     }
-    for (; q < b; q++) {
+    // steps q .. b-1; the value appended at step q is s[q+7].  Loads run
+    // eight steps ahead through a register ring (static indices by unrolling).
+    float pre[8];
+#pragma unroll
+    for (int t = 0; t < 8; t++) pre[t] = (q + 7 + t < n) ? s[(long long)(q + 7 + t) * st] : 0.f;
+    for (; q + 8 <= b; q += 8) {
+#pragma unroll
+        for (int t = 0; t < 8; t++) {
+            const int qq = q + t;
+            const float v = pass2_f(w, f);
+            if (qq >= a) o[(long long)qq * st] = v + cr[qq];
+#pragma unroll
+            for (int u = 0; u < 5; u++) w[u] = w[u + 1];
+            w[5] = v;
+#pragma unroll
+            for (int u = 6; u < 12; u++) w[u] = w[u + 1];
+            w[12] = pre[t];
+            pre[t] = (qq + 15 < n) ? s[(long long)(qq + 15) * st] : 0.f;
+        }
+    }
+    for (int t = 0; q < b; q++, t++) {
         const float v = pass2_f(w, f);
         if (q >= a) o[(long long)q * st] = v + cr[q];
 #pragma unroll
-        for (int t = 0; t < 5; t++) w[t] = w[t + 1];
+        for (int u = 0; u < 5; u++) w[u] = w[u + 1];
         w[5] = v;
 #pragma unroll
-        for (int t = 6; t < 12; t++) w[t] = w[t + 1];
+        for (int u = 6; u < 12; u++) w[u] = w[u + 1];
         w[12] = (q + 7 < n) ? s[(long long)(q + 7) * st] : 0.f;
     }
     if (c == chunks - 1) {
@@ -551,7 +586,7 @@ cudaError_t launch_split_kernel(ns_ctx *c, int cls, int stage, cudaStream_t s)
     k_split_stage<FIRST, SRC><<<grd, blk, 0, s>>>(d, sp.fpitch, qa, qb, c->W, sp.xc, sp.yc,    \
                                                   sp.xcl, sp.ycl, sp.mean, sp.sigx, sp.sigy,   \
                                                   sp.src,                                      \
-                                                  c->stage_sin, c->p.dt, c->alpha[stage],      \
+                                                  c->stage_sin, (float)c->p.dt, c->alpha[stage], \
                                                   c->beta[stage], stage)
         if (stage == 0) {
             if (src) NS_SPL(true, true); else NS_SPL(true, false);
