@@ -211,6 +211,37 @@ NS_API const char *ns_kernel_name(int kernel_class);
 NS_API int ns_fp64_peak(int device, double *tflops);
 
 /*
+ * Batched sweeps: many independent Euler instances (inviscid = 1, nk = 4,
+ * base flow uniform in x with v = 0 and uniform p; each with its own size,
+ * metric, buffer, time step and source) advanced together, one cooperative
+ * persistent kernel per step (captured in a CUDA graph) whose phases run over
+ * a work list spanning every instance.  Each instance follows rk_euler
+ * (rk.f90:12-75) exactly as ns_step does; precision NS_PREC_FP64 or
+ * NS_PREC_SPLIT.  All instances share one sigmaf and one device.
+ */
+typedef struct ns_batch ns_batch;
+NS_API int ns_batch_create(const ns_params *const *params, int n, int precision, ns_batch **out);
+NS_API void ns_batch_destroy(ns_batch *b);
+NS_API int ns_batch_set_state(ns_batch *b, int instance, const double *U, int layout);
+NS_API int ns_batch_get_state(ns_batch *b, int instance, double *U, int layout);
+NS_API int ns_batch_step(ns_batch *b, int iter0, int nsteps);
+/* Waits for the batch's work; NS_ERR_TIMEOUT if a phase barrier gave up. */
+NS_API int ns_batch_synchronize(ns_batch *b);
+NS_API int ns_batch_set_stream(ns_batch *b, void *stream);
+/* Tile autotuner: times every tile height (8, 16 rows) and residency for
+ * `reps` steps on the current state (advancing it), keeps the fastest. */
+NS_API int ns_batch_autotune(ns_batch *b, int iter0, int reps, int *tile_rows,
+                             int *blocks_per_sm, double *ms_per_step);
+/* Current launch shape: grid blocks, tile rows, blocks per SM, and the work
+ * items per phase items[4] = {tiles, x lines, y lines, instances}. */
+NS_API int ns_batch_info(ns_batch *b, int *grid, int *tile_rows, int *blocks_per_sm,
+                         int *items);
+/* Failure-detection hook: one step whose barriers wait for `extra` blocks
+ * that do not exist, each wait bounded by spin_limit spins; returns
+ * NS_ERR_TIMEOUT and leaves the batch and its state usable. */
+NS_API int ns_batch_barrier_test(ns_batch *b, int extra, long long spin_limit);
+
+/*
  * ns_step_noalloc -- the time step for callers that cannot allocate device
  * memory.  No counterpart in the reference: it is an addition for hosts
  * whose device memory belongs to something else (a framework or pool that

@@ -8,7 +8,7 @@ and the reference-shaped solver interface (`Solver`).
 from . import _lib
 from .cases import (Case, acoustic_pulse_case, init_dados, mixing_layer_case,
                     stretched_ns_case, uniform_flow_case)
-from .solver import Solver
+from .solver import Batch, Solver
 
-__all__ = ["Case", "Solver", "acoustic_pulse_case", "init_dados", "mixing_layer_case",
+__all__ = ["Batch", "Case", "Solver", "acoustic_pulse_case", "init_dados", "mixing_layer_case",
            "stretched_ns_case", "uniform_flow_case", "_lib"]

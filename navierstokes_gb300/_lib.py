@@ -56,6 +56,18 @@ SIGNATURES = [
     ("ns_kernel_name", C.c_char_p, [C.c_int]),
     ("ns_fp64_peak", C.c_int, [C.c_int, C.POINTER(C.c_double)]),
     ("ns_step_noalloc", C.c_int, [_VP, _VP, C.c_int64, C.c_int, C.c_int, _VP]),
+    ("ns_batch_create", C.c_int, [_VP, C.c_int, C.c_int, C.POINTER(_VP)]),
+    ("ns_batch_destroy", None, [_VP]),
+    ("ns_batch_set_state", C.c_int, [_VP, C.c_int, _VP, C.c_int]),
+    ("ns_batch_get_state", C.c_int, [_VP, C.c_int, _VP, C.c_int]),
+    ("ns_batch_step", C.c_int, [_VP, C.c_int, C.c_int]),
+    ("ns_batch_synchronize", C.c_int, [_VP]),
+    ("ns_batch_set_stream", C.c_int, [_VP, _VP]),
+    ("ns_batch_autotune", C.c_int, [_VP, C.c_int, C.c_int, C.POINTER(C.c_int),
+                                    C.POINTER(C.c_int), C.POINTER(C.c_double)]),
+    ("ns_batch_info", C.c_int, [_VP, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                C.POINTER(C.c_int), _VP]),
+    ("ns_batch_barrier_test", C.c_int, [_VP, C.c_int, C.c_longlong]),
 ]
 
 NS_KC_COUNT = 11

@@ -326,6 +326,36 @@ def stretched_ns_case(imax=4096, jmax=2048, nk=4, D=40, sigmaf=0.2, mach=0.5, Re
                       "vortex, dt = min(CFL 0.5, viscous limit) (new hook)")
 
 
+def sweep_cases(n=64, seed=0, nmin=128, nmax=1024, D=30, sigmaf=0.2, cfl=0.5, steps=300,
+                quirk_buffer=True):
+    """The parameter sweep of many independent Euler instances: sizes
+    Nx, Ny = 32*round(exp(U[ln nmin, ln nmax])/32), a time-harmonic monopole
+    S = A*sin(omega*t)*exp(-ln2*r^2/3^2) at the centre (the form of
+    rk.f90:188-189, with stage time) with A ~ U[1e-4, 1e-2] and
+    omega ~ U[0.2, 1.0], and a uniform mean flow M ~ U[0, 0.6] along x.
+    Uniform grids with dx = dy = 1, quiescent start, dt = cfl/(M+1).
+    Draws come from numpy.random.default_rng(seed) in this order: Nx, Ny, A,
+    omega, M (each an array of n)."""
+    rng = np.random.default_rng(seed)
+    lo, hi = math.log(nmin), math.log(nmax)
+    nx = (32 * np.round(np.exp(rng.uniform(lo, hi, n)) / 32)).astype(int)
+    ny = (32 * np.round(np.exp(rng.uniform(lo, hi, n)) / 32)).astype(int)
+    amp = rng.uniform(1e-4, 1e-2, n)
+    omega = rng.uniform(0.2, 1.0, n)
+    mach = rng.uniform(0.0, 0.6, n)
+    out = []
+    for q in range(n):
+        c = uniform_flow_case(imax=int(nx[q]), jmax=int(ny[q]), mach=float(mach[q]), D=D,
+                              sigmaf=sigmaf, pulse_amp=0.0, vortex_eps=0.0, cfl=cfl,
+                              steps=steps, quirk_buffer=quirk_buffer)
+        c.name = f"sweep{q}_{c.imax}x{c.jmax}"
+        c.source_mode = L.NS_SRC_GAUSSIAN
+        c.amplitude, c.wf, c.m_pt, c.n_pt, c.r0 = float(amp[q]), float(omega[q]), 0.0, 0.0, 3.0
+        c.notes = f"sweep instance {q} (seed {seed}): A={amp[q]:.3g} omega={omega[q]:.3g} M={mach[q]:.3g}"
+        out.append(c)
+    return out
+
+
 def params_from_case(case: Case, device: int = 0, precision: int = L.NS_PREC_FP64):
     """Fills an ns_params for `case`; returns (params, keep-alive arrays)."""
     lib = L.load()

@@ -1,0 +1,1466 @@
+// ns_batch.cu -- many independent instances of the time step in one
+// persistent launch per step.
+//
+// A parameter sweep advances dozens of uneven-size Euler grids (each one a
+// complete rk_euler, rk.f90:12-75, with its own size, source, mean flow and
+// time step).  One cooperative, persistent kernel per step runs the six
+// stages; each stage has four phases over a work list that spans every
+// instance:
+//   A  tiles:   FP32/FP64 derivatives from a shared-memory tile, Euler RHS,
+//               FP64 LDDRK update, buffer                (rk.f90:52-64)
+//   B  x lines: lddfilterx                                (filtering.f90:9-96)
+//   C  y lines: lddfiltery                                (filtering.f90:98-190)
+//   D  edges:   ccpml                                     (cc.f90:6-68)
+// separated by grid-wide barriers.  Every barrier wait is bounded: a block
+// that waits too long sets an error word and returns, the others see the
+// word and return too, and the host reports NS_ERR_TIMEOUT.
+//
+// Each instance is written as U = Ub + q' with Ub its base flow (uniform in
+// x, v = 0, uniform p); T = float stores q' in FP32 (split precision),
+// T = double in FP64.  The arithmetic is that of the single-grid split path
+// (ns_split.cu), instance by instance.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "ns_internal.cuh"
+
+namespace ns {
+namespace batch {
+
+struct Inst {
+    int imax, jmax, pitch, D;  // pitch in elements of T and of W
+    long long q_off;           // plane 0 of the instance in q[0], q[1]
+    long long w_off;           // plane 0 in W (FP64)
+    long long s_off;           // source field (-1: none)
+    int x_off, y_off;          // per-column / per-row table offsets
+    int fx_chunks, fy_chunks, warm;
+    float dt_f, pmean_f, gamma_f, p_bc_f;
+    double dt_d, pmean_d, gamma_d, p_bc_d;
+};
+
+struct Args {
+    const Inst *inst;
+    const int4 *tiles, *fx, *fy;
+    const int *bc;
+    int ntiles, nfx, nfy, nbc;
+    void *q0, *q1;             // T*
+    double *W;
+    // tables in the state's precision T (xcl, ycl: FP32 low parts, split only)
+    const void *xc, *yc, *sigx, *sigy, *rho_bc, *mrho, *mu, *mdrho, *mdu, *corr;
+    const float *xcl, *ycl;
+    const void *src;           // T*
+    const double *stage_sin;   // [inst][8]
+    double alpha[6], beta[6];
+    // filter coefficients ([0] = x, [1] = y) in both precisions
+    float fm_f[7], fbm1_f[2], fb_f[2][6], fbsum_f[2];
+    double fm_d[7], fbm1_d[2], fb_d[2][6], fbsum_d[2];
+    unsigned *bar_count, *bar_gen;
+    int *err;
+    unsigned nblocks;          // blocks that take part in each barrier
+    long long spin_limit;
+};
+
+constexpr int kTX = 32, kH = 3, kWarps = 8;
+
+template <typename T>
+__device__ __forceinline__ T pick(float f, double d);
+template <>
+__device__ __forceinline__ float pick<float>(float f, double) { return f; }
+template <>
+__device__ __forceinline__ double pick<double>(float, double d) { return d; }
+
+template <typename T>
+__device__ __forceinline__ const T *tab(const void *p) { return static_cast<const T *>(p); }
+
+template <typename T>
+__device__ __forceinline__ double to_d(T x);
+template <>
+__device__ __forceinline__ double to_d<double>(double x) { return x; }
+
+__device__ __forceinline__ double f2d_exact(float x)
+{
+    const unsigned b = __float_as_uint(x);
+    const unsigned e = (b >> 23) & 0xffu;
+    if ((b & 0x7fffffffu) == 0u) return __hiloint2double((int)(b & 0x80000000u), 0);
+    if (e == 0u || e == 0xffu) return (double)x;
+    const unsigned m = b & 0x7fffffu;
+    const unsigned hi = (b & 0x80000000u) | ((e + (1023u - 127u)) << 20) | (m >> 3);
+    return __hiloint2double((int)hi, (int)(m << 29));
+}
+template <>
+__device__ __forceinline__ double to_d<float>(float x) { return f2d_exact(x); }
+
+template <typename T>
+__device__ __forceinline__ T from_d(double x);
+template <>
+__device__ __forceinline__ double from_d<double>(double x) { return x; }
+template <>
+__device__ __forceinline__ float from_d<float>(double x)
+{
+    const unsigned hi = (unsigned)__double2hiint(x);
+    const unsigned lo = (unsigned)__double2loint(x);
+    const unsigned e = (hi >> 20) & 0x7ffu;
+    if (e < 1023u - 126u || e > 1023u + 127u) {
+        if (((hi & 0x7fffffffu) | lo) == 0u) return __uint_as_float(hi & 0x80000000u);
+        return (float)x;
+    }
+    const unsigned top = ((hi & 0xfffffu) << 3) | (lo >> 29);
+    const unsigned rest = lo & 0x1fffffffu;
+    unsigned f = (hi & 0x80000000u) | ((e - (1023u - 127u)) << 23) | top;
+    if (rest > (1u << 28) || (rest == (1u << 28) && (top & 1u))) f += 1u;
+    return __uint_as_float(f);
+}
+
+// Grid-wide barrier with a bounded wait.  Returns false when this or another
+// block gave up (the error word is set), after which callers return.
+__device__ __forceinline__ bool grid_barrier(const Args &a)
+{
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = (*(volatile int *)a.err == 0);
+        if (ok) {
+            const unsigned g = *(volatile unsigned *)a.bar_gen;
+            __threadfence();
+            if (atomicAdd(a.bar_count, 1u) == a.nblocks - 1u) {
+                atomicExch(a.bar_count, 0u);
+                __threadfence();
+                atomicAdd(a.bar_gen, 1u);
+            } else {
+                long long spins = 0;
+                while (*(volatile unsigned *)a.bar_gen == g) {
+                    if (*(volatile int *)a.err != 0) { ok = 0; break; }
+                    if (++spins > a.spin_limit) {
+                        atomicExch(a.err, 1);
+                        ok = 0;
+                        break;
+                    }
+                    __nanosleep(64);
+                }
+            }
+            __threadfence();
+        }
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// ---------------------------------------------------------------------------
+// Phase A: one tile of one instance.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
+{
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// The state buffers are written by other phases of the same launch, so they
+// are read through plain (coherent) loads: no __restrict__ / read-only path.
+template <typename T, int TY>
+__device__ void stage_tile(const Args &a, int st, int4 item, const T *qin, T *qout,
+                           unsigned char *smem)
+{
+    constexpr int SW = kTX + 2 * kH, SH = TY + 2 * kH;
+    T(*sq)[SH][SW] = reinterpret_cast<T(*)[SH][SW]>(smem);
+    const Inst in = a.inst[item.x];
+    const int i0 = item.y, j0 = item.z;
+    const long long plane = (long long)in.pitch * in.jmax;
+    const T *q = qin + in.q_off;
+    T *qo = qout + in.q_off;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    for (int r = ty; r < SH; r += kWarps) {
+        const int gj = j0 - kH + r;
+        const bool rowok = gj >= 0 && gj < in.jmax;
+        for (int cc = tx; cc < SW; cc += kTX) {
+            const int gi = i0 - kH + cc;
+            const bool ok = rowok && gi >= 0 && gi < in.imax;
+            const long long g = (long long)gj * in.pitch + gi;
+#pragma unroll
+            for (int k = 0; k < 4; k++) sq[k][r][cc] = ok ? q[k * plane + g] : T(0);
+        }
+    }
+    __syncthreads();
+    const int i = i0 + tx;
+    if (i < in.imax) {
+        const T *cxp = tab<T>(a.xc) + (long long)kCoefStride * (in.x_off + i);
+        const float *cxl = a.xcl + (long long)kCoefStride * (in.x_off + i);
+        const bool xint = (i >= 3 && i < in.imax - 3);
+        const T ssin = (T)a.stage_sin[item.x * 8 + st];
+#pragma unroll
+        for (int h = 0; h < TY / kWarps; h++) {
+            const int ly = ty + kWarps * h;
+            const int j = j0 + ly;
+            if (j >= in.jmax) break;
+            const long long idx = (long long)j * in.pitch + i;
+            const int sr = ly + kH, sc = tx + kH;
+            const T *cyp = tab<T>(a.yc) + (long long)kCoefStride * (in.y_off + j);
+            const float *cyl = a.ycl + (long long)kCoefStride * (in.y_off + j);
+            const bool yint = (j >= 3 && j < in.jmax - 3);
+            T qv[4], gx[4], gy[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                qv[k] = sq[k][sr][sc];
+                if (xint) {
+                    T r = cxp[4] * (sq[k][sr][sc + 1] - sq[k][sr][sc - 1]);
+                    r = fma(cxp[5], sq[k][sr][sc + 2] - sq[k][sr][sc - 2], r);
+                    gx[k] = fma(cxp[6], sq[k][sr][sc + 3] - sq[k][sr][sc - 3], r);
+                } else {
+                    const int o0 = (i < 3) ? -i : (in.imax - 7 - i);
+                    const T *g = q + k * plane + idx + o0;
+                    const T f0 = q[k * plane + idx];
+                    T r = T(0);
+#pragma unroll
+                    for (int z = 0; z < 7; z++) {
+                        r = fma(cxp[z], g[z] - f0, r);
+                    }
+                    gx[k] = r;
+                }
+                if (yint) {
+                    T r = cyp[4] * (sq[k][sr + 1][sc] - sq[k][sr - 1][sc]);
+                    r = fma(cyp[5], sq[k][sr + 2][sc] - sq[k][sr - 2][sc], r);
+                    gy[k] = fma(cyp[6], sq[k][sr + 3][sc] - sq[k][sr - 3][sc], r);
+                } else {
+                    const int o0 = (j < 3) ? -j : (in.jmax - 7 - j);
+                    const T *g = q + k * plane + idx + (long long)o0 * in.pitch;
+                    const T f0 = q[k * plane + idx];
+                    T r = T(0);
+#pragma unroll
+                    for (int z = 0; z < 7; z++) {
+                        r = fma(cyp[z], g[(long long)z * in.pitch] - f0, r);
+                    }
+                    gy[k] = r;
+                }
+            }
+            const bool interior = (i > 0) && (i < in.imax - 1) && (j > 0) && (j < in.jmax - 1);
+            if (interior) {
+                T div = gx[1] + gy[2];
+                if constexpr (sizeof(T) == 4) if (xint && yint) {
+                    // compensated divergence, as the single-grid split path
+                    float xh = 0.f, xl = 0.f, yh = 0.f, yl = 0.f;
+#pragma unroll
+                    for (int s = 1; s <= 3; s++) {
+                        float dh, dl, sh, se;
+                        two_sum((float)sq[1][sr][sc + s], -(float)sq[1][sr][sc - s], dh, dl);
+                        float ph = cxp[3 + s] * dh;
+                        float pl = fmaf(cxp[3 + s], dh, -ph) + fmaf(cxp[3 + s], dl, cxl[3 + s] * dh);
+                        two_sum(xh, ph, sh, se);
+                        xh = sh;
+                        xl += se + pl;
+                        two_sum((float)sq[2][sr + s][sc], -(float)sq[2][sr - s][sc], dh, dl);
+                        ph = cyp[3 + s] * dh;
+                        pl = fmaf(cyp[3 + s], dh, -ph) + fmaf(cyp[3 + s], dl, cyl[3 + s] * dh);
+                        two_sum(yh, ph, sh, se);
+                        yh = sh;
+                        yl += se + pl;
+                    }
+                    float sh, se;
+                    two_sum(xh, yh, sh, se);
+                    div = T(sh + (se + (xl + yl)));
+                }
+                const int yo = in.y_off + j;
+                const T rho = tab<T>(a.mrho)[yo] + qv[0];
+                const T uu = tab<T>(a.mu)[yo] + qv[1];
+                const T vv = qv[2];
+                const T pp = pick<T>(in.pmean_f, in.pmean_d) + qv[3];
+                const T rhoy = tab<T>(a.mdrho)[yo] + gy[0];
+                const T uy = tab<T>(a.mdu)[yo] + gy[1];
+                const T ri = T(1) / rho;
+                T r[4];
+                T t = uu * gx[0];
+                t = fma(vv, rhoy, t);
+                t = fma(rho, div, t);
+                r[0] = -t;
+                t = uu * gx[1];
+                t = fma(ri, gx[3], t);
+                t = fma(vv, uy, t);
+                r[1] = -t;
+                t = uu * gx[2];
+                t = fma(vv, gy[2], t);
+                t = fma(ri, gy[3], t);
+                r[2] = -t;
+                const T gp = pick<T>(in.gamma_f, in.gamma_d) * pp;
+                t = uu * gx[3];
+                t = fma(vv, gy[3], t);
+                t = fma(gp, div, t);
+                if (in.s_off >= 0) {
+                    const T *src = reinterpret_cast<const T *>(a.src) + in.s_off;
+                    t = t - ssin * src[idx];
+                }
+                r[3] = -t;
+                double *Wp = a.W + in.w_off + idx;
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    const double dr = to_d<T>(pick<T>(in.dt_f, in.dt_d) * r[k]);
+                    const double w = (st == 0) ? dr : fma(a.alpha[st], Wp[k * plane], dr);
+                    Wp[k * plane] = w;
+                    qv[k] = from_d<T>(fma(a.beta[st], w, to_d<T>(qv[k])));
+                }
+            }
+            if (j < in.D || j >= in.jmax - in.D) {
+                const T s = tab<T>(a.sigy)[in.y_off + j];
+#pragma unroll
+                for (int k = 0; k < 4; k++) qv[k] *= s;
+            }
+            if (i < in.D || i >= in.imax - in.D) {
+                const T s = tab<T>(a.sigx)[in.x_off + i];
+#pragma unroll
+                for (int k = 0; k < 4; k++) qv[k] *= s;
+            }
+#pragma unroll
+            for (int k = 0; k < 4; k++) qo[k * plane + idx] = qv[k];
+        }
+    }
+    __syncthreads();  // the tile buffer is reused by the next item
+}
+
+// ---------------------------------------------------------------------------
+// Filter recurrences (constant-exact forms of ns_split.cu).
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ T pass2(const T *w, const T *m)
+{
+    const T u0 = w[6];
+    T acc = m[6] * ((w[12] - u0) + (w[0] - u0));
+    acc = fma(m[5], (w[11] - u0) + (w[1] - u0), acc);
+    acc = fma(m[4], (w[10] - u0) + (w[2] - u0), acc);
+    acc = fma(m[3], (w[9] - u0) + (w[3] - u0), acc);
+    acc = fma(m[2], (w[8] - u0) + (w[4] - u0), acc);
+    acc = fma(m[1], w[7] - u0, acc);
+    return fma(m[1], w[5] - u0, u0 + acc);
+}
+
+template <typename T, int DIR>
+__device__ __forceinline__ T passb(const T *w, int p, T bm1, const T *b, T bsum)
+{
+    const T u0 = w[p];
+    T acc = bsum * u0;
+#pragma unroll
+    for (int z = 1; z <= 5; z++) acc = fma(b[z], w[p + DIR * z] - u0, acc);
+    return fma(bm1, w[p - DIR] - u0, u0 + acc);
+}
+
+template <typename T>
+struct FCoef {
+    const T *m, *b;
+    T bm1, bsum;
+};
+template <typename T>
+__device__ __forceinline__ FCoef<T> fcoef(const Args &a, int d);
+template <>
+__device__ __forceinline__ FCoef<float> fcoef<float>(const Args &a, int d)
+{
+    return {a.fm_f, a.fb_f[d], a.fbm1_f[d], a.fbsum_f[d]};
+}
+template <>
+__device__ __forceinline__ FCoef<double> fcoef<double>(const Args &a, int d)
+{
+    return {a.fm_d, a.fb_d[d], a.fbm1_d[d], a.fbsum_d[d]};
+}
+
+// Phase C: y lines of 32 consecutive columns (one per lane).
+template <typename T>
+__device__ void fy_item(const Args &a, int4 item, const T *srcq, T *dstq)
+{
+    const Inst in = a.inst[item.x];
+    const int k = item.y, col = item.z + (threadIdx.x & 31), c = item.w;
+    if (col >= in.imax) return;
+    const int n = in.jmax, chunks = in.fy_chunks, warm = in.warm;
+    const long long st = in.pitch;
+    const long long base = in.q_off + (long long)k * in.pitch * in.jmax + col;
+    const T *s = srcq + base;
+    T *o = dstq + base;
+    const T *cr = tab<T>(a.corr) + 4LL * in.y_off + (long long)k * n;  // [k][j] of this instance
+    const FCoef<T> fc = fcoef<T>(a, 1);
+    const int len2 = n - 12;
+    const int a0 = 6 + (int)(((long long)c * len2) / chunks);
+    const int b0 = 6 + (int)(((long long)(c + 1) * len2) / chunks);
+    T w[13];
+    int q;
+    if (c == 0 || warm < 0 || a0 - warm <= 6) {
+#pragma unroll
+        for (int t = 0; t < 13; t++) w[t] = s[t * st];
+#pragma unroll
+        for (int p = 1; p <= 6; p++) w[p] = passb<T, 1>(w, p, fc.bm1, fc.b, fc.bsum);
+        if (c == 0)
+            for (int p = 0; p < 6; p++) o[p * st] = w[p] + cr[p];
+        q = 6;
+    } else {
+        q = a0 - warm;
+#pragma unroll
+        for (int t = 0; t < 13; t++) w[t] = s[(long long)(q - 6 + t) * st];
+    }
+    for (; q < b0; q++) {
+        const T v = pass2<T>(w, fc.m);
+        if (q >= a0) o[(long long)q * st] = v + cr[q];
+#pragma unroll
+        for (int u = 0; u < 5; u++) w[u] = w[u + 1];
+        w[5] = v;
+#pragma unroll
+        for (int u = 6; u < 12; u++) w[u] = w[u + 1];
+        w[12] = (q + 7 < n) ? s[(long long)(q + 7) * st] : T(0);
+    }
+    if (c == chunks - 1) {
+#pragma unroll
+        for (int x = 10; x >= 5; x--) w[x] = passb<T, -1>(w, x, fc.bm1, fc.b, fc.bsum);
+        for (int x = 5; x < 12; x++) o[(long long)(n - 12 + x) * st] = w[x] + cr[n - 12 + x];
+    }
+}
+
+// Phase B: x lines of 32 consecutive rows, staged through shared memory
+// PW positions at a time (coalesced row segments).
+template <typename T, int PW>
+__device__ void fx_item(const Args &a, int4 item, const T *srcq, T *dstq, T (*ti)[PW + 1],
+                        T (*to)[PW + 1])
+{
+    const Inst in = a.inst[item.x];
+    const int lane = threadIdx.x & 31;
+    const int k = item.y, row0 = item.z, c = item.w;
+    const int n = in.imax, chunks = in.fx_chunks, warm = in.warm;
+    const int nrows = min(32, in.jmax - row0);
+    const long long base = in.q_off + (long long)k * in.pitch * in.jmax + (long long)row0 * in.pitch;
+    const T *sb = srcq + base;
+    T *ob = dstq + base;
+    const bool active = lane < nrows;
+    const T *s = sb + (long long)(active ? lane : 0) * in.pitch;
+    const int len2 = n - 12;
+    const int a0 = 6 + (int)(((long long)c * len2) / chunks);
+    const int b0 = 6 + (int)(((long long)(c + 1) * len2) / chunks);
+    const bool exact = (c == 0 || warm < 0 || a0 - warm <= 6);
+    const int q0 = exact ? 6 : a0 - warm;
+    const FCoef<T> fc = fcoef<T>(a, 0);
+    T w[13];
+    if (exact) {
+#pragma unroll
+        for (int t = 0; t < 13; t++) w[t] = s[t];
+#pragma unroll
+        for (int p = 1; p <= 6; p++) w[p] = passb<T, 1>(w, p, fc.bm1, fc.b, fc.bsum);
+        if (c == 0 && active)
+            for (int p = 0; p < 6; p++) ob[(long long)lane * in.pitch + p] = w[p];
+    } else {
+#pragma unroll
+        for (int t = 0; t < 13; t++) w[t] = s[q0 - 6 + t];
+    }
+    for (int qb = q0; qb < b0; qb += PW) {
+        const int pin = qb + 7;
+        for (int r = 0; r < nrows; r++)
+            for (int x = lane; x < PW; x += 32) {
+                const int pos = pin + x;
+                ti[r][x] = (pos < n) ? sb[(long long)r * in.pitch + pos] : T(0);
+            }
+        __syncwarp();
+        const int nstep = min(PW, b0 - qb);
+        for (int t = 0; t < nstep; t++) {
+            const T v = pass2<T>(w, fc.m);
+            to[lane][t] = v;
+#pragma unroll
+            for (int u = 0; u < 5; u++) w[u] = w[u + 1];
+            w[5] = v;
+#pragma unroll
+            for (int u = 6; u < 12; u++) w[u] = w[u + 1];
+            w[12] = ti[lane][t];
+        }
+        __syncwarp();
+        for (int r = 0; r < nrows; r++)
+            for (int x = lane; x < PW; x += 32) {
+                const int qq = qb + x;
+                if (x < nstep && qq >= a0) ob[(long long)r * in.pitch + qq] = to[r][x];
+            }
+        __syncwarp();
+    }
+    if (c == chunks - 1 && active) {
+#pragma unroll
+        for (int x = 10; x >= 5; x--) w[x] = passb<T, -1>(w, x, fc.bm1, fc.b, fc.bsum);
+        for (int x = 5; x < 12; x++) ob[(long long)lane * in.pitch + (n - 12 + x)] = w[x];
+    }
+}
+
+// Phase D: ccpml of one instance, one warp.
+template <typename T>
+__device__ void bc_item(const Args &a, int inst, T *qall)
+{
+    const Inst in = a.inst[inst];
+    const long long P = (long long)in.pitch * in.jmax;
+    T *q = qall + in.q_off;
+    const T pbc = pick<T>(in.p_bc_f, in.p_bc_d);
+    const T *rbc = tab<T>(a.rho_bc) + in.y_off;
+    auto colval = [&](int i, int j, T *v) {
+        const long long r = (long long)j * in.pitch;
+        if (i == 0) {
+            v[0] = rbc[j];
+            v[1] = T(2) * q[P + r + 1] - q[P + r + 2];
+            v[2] = T(0);
+            v[3] = pbc;
+        } else {
+            for (int k = 0; k < 3; k++) v[k] = T(2) * q[k * P + r + in.imax - 2] - q[k * P + r + in.imax - 3];
+            v[3] = pbc;
+        }
+    };
+    const int nt = max(in.imax, in.jmax);
+    for (int t = threadIdx.x & 31; t < nt; t += 32) {
+        T v[4];
+        if (t > 0 && t < in.jmax - 1) {
+            const long long r = (long long)t * in.pitch;
+            colval(0, t, v);
+            for (int k = 0; k < 4; k++) q[k * P + r] = v[k];
+            colval(in.imax - 1, t, v);
+            for (int k = 0; k < 4; k++) q[k * P + r + in.imax - 1] = v[k];
+        }
+        if (t < in.imax) {
+            const int jt = in.jmax - 1;
+            T x[4], y[4];
+            if (t == 0 || t == in.imax - 1) {
+                colval(t, jt - 1, x);
+                colval(t, jt - 2, y);
+            } else {
+                for (int k = 0; k < 4; k++) {
+                    x[k] = q[k * P + (long long)(jt - 1) * in.pitch + t];
+                    y[k] = q[k * P + (long long)(jt - 2) * in.pitch + t];
+                }
+            }
+            for (int k = 0; k < 3; k++) q[k * P + (long long)jt * in.pitch + t] = T(2) * x[k] - y[k];
+            q[3 * P + (long long)jt * in.pitch + t] = pbc;
+            if (t == 0 || t == in.imax - 1) {
+                colval(t, 1, x);
+                colval(t, 2, y);
+            } else {
+                for (int k = 0; k < 4; k++) {
+                    x[k] = q[k * P + in.pitch + t];
+                    y[k] = q[k * P + 2LL * in.pitch + t];
+                }
+            }
+            for (int k = 0; k < 3; k++) q[k * P + t] = T(2) * x[k] - y[k];
+            q[3 * P + t] = pbc;
+        }
+    }
+}
+
+template <typename T, int TY>
+__global__ void __launch_bounds__(256) k_batch_step(Args a)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    constexpr int PW = sizeof(T) == 4 ? 32 : 16;
+    const int warp = threadIdx.x >> 5;
+    T(*ti)[PW + 1] = reinterpret_cast<T(*)[PW + 1]>(smem) + (size_t)warp * 2 * 32;
+    T(*to)[PW + 1] = ti + 32;
+    const long long nwarps = (long long)gridDim.x * kWarps;
+    const long long gw = (long long)blockIdx.x * kWarps + warp;
+    for (int st = 0; st < 6; st++) {
+        T *qa = reinterpret_cast<T *>((st & 1) ? a.q1 : a.q0);
+        T *qb = reinterpret_cast<T *>((st & 1) ? a.q0 : a.q1);
+        for (int it = blockIdx.x; it < a.ntiles; it += gridDim.x)
+            stage_tile<T, TY>(a, st, a.tiles[it], qa, qb, smem);
+        if (!grid_barrier(a)) return;
+        for (long long wi = gw; wi < a.nfx; wi += nwarps) fx_item<T, PW>(a, a.fx[wi], qb, qa, ti, to);
+        if (!grid_barrier(a)) return;
+        for (long long wi = gw; wi < a.nfy; wi += nwarps) fy_item<T>(a, a.fy[wi], qa, qb);
+        if (!grid_barrier(a)) return;
+        for (long long wi = gw; wi < a.nbc; wi += nwarps) bc_item<T>(a, a.bc[wi], qb);
+        if (st < 5 && !grid_barrier(a)) return;
+    }
+}
+
+__global__ void k_batch_sin(const double *wf, const double *dt, int n, int *d_iter, double *ss)
+{
+    const int t = threadIdx.x;
+    const int iter = *d_iter;
+    // rk.f90:188: sin(wf*((iter+c_k)*dt)) per instance and stage
+    const double ct[6] = {0.0, 0.032918605146, 0.249351723343,
+                          0.466911705055, 0.582030414044, 0.847252983783};
+    for (int e = t; e < n * 6; e += blockDim.x) {
+        const int in = e / 6, k = e % 6;
+        ss[in * 8 + k] = sin(wf[in] * (((double)iter + ct[k]) * dt[in]));
+    }
+    __syncthreads();
+    if (t == 0) *d_iter = iter + 1;
+}
+
+__global__ void k_batch_set_iter(int *d_iter, int v) { *d_iter = v; }
+
+template <typename T>
+__global__ void k_batch_from_full(const double *U, int imax, int jmax, int upitch,
+                                  const double *rho, const double *u, double pmean, T *q,
+                                  int pitch)
+{
+    // U: host-uploaded FP64 planes (upitch), q' = U - Ub with Ub(j) = (rho, u, 0, pmean)
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= imax || j >= jmax) return;
+    const double base[4] = {rho[j], u[j], 0.0, pmean};
+    for (int k = 0; k < 4; k++)
+        q[(long long)k * pitch * jmax + (long long)j * pitch + i] =
+            (T)(U[(long long)k * upitch * jmax + (long long)j * upitch + i] - base[k]);
+}
+
+template <typename T>
+__global__ void k_batch_to_full(const T *q, int imax, int jmax, int pitch, const double *rho,
+                                const double *u, double pmean, double *U, int upitch)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= imax || j >= jmax) return;
+    const double base[4] = {rho[j], u[j], 0.0, pmean};
+    for (int k = 0; k < 4; k++)
+        U[(long long)k * upitch * jmax + (long long)j * upitch + i] =
+            base[k] + (double)q[(long long)k * pitch * jmax + (long long)j * pitch + i];
+}
+
+}  // namespace batch
+}  // namespace ns
+
+// ===========================================================================
+// Host side
+// ===========================================================================
+struct ns_batch {
+    int n = 0, dev = 0, precision = NS_PREC_FP64;
+    cudaStream_t own = nullptr, stream = nullptr;
+    std::vector<ns::batch::Inst> hinst;
+    std::vector<double> hrho, hu;                 // per-row base flow, pooled
+    std::vector<double> hpmean;
+    size_t qsize = 0, wsize = 0;                  // elements
+    void *q[2] = {nullptr, nullptr};
+    double *W = nullptr, *stage_sin = nullptr, *wf = nullptr, *dtv = nullptr;
+    double *drho = nullptr, *du = nullptr;        // FP64 per-row base flow for conversions
+    double *stagebuf = nullptr;                   // FP64 staging planes for host transfers
+    size_t stagebuf_elems = 0;
+    ns::batch::Inst *inst = nullptr;
+    int4 *tiles[2] = {nullptr, nullptr}, *fx = nullptr, *fy = nullptr;
+    int ntiles[2] = {0, 0}, nfx = 0, nfy = 0, nbc = 0;
+    int *bc = nullptr;
+    void *xc = nullptr, *yc = nullptr, *sigx = nullptr, *sigy = nullptr, *rho_bc = nullptr,
+         *mrho = nullptr, *mu = nullptr, *mdrho = nullptr, *mdu = nullptr, *corr = nullptr;
+    float *xcl = nullptr, *ycl = nullptr;
+    void *src = nullptr;
+    unsigned *bar = nullptr;   // [0] count, [1] generation
+    int *err = nullptr;
+    int *d_iter = nullptr;
+    ns::batch::Args args{};
+    int ty = 16, blocks_per_sm = 0, grid = 0;
+    size_t smem = 0;
+    double tuned_ms = 0.0;
+    bool has_src = false, have_state = false;
+    bool no_graph = false;    // capture of the cooperative launch unavailable
+    cudaGraphExec_t exec = nullptr;
+    std::string err_text;
+};
+
+namespace {
+
+const double kA[3] = {0.770882380518, -0.166705904415, 0.0208431427703};
+const double kA4[7] = {0.049041958000, -0.46884035700, -0.47476091400, 1.27327473700,
+                       -0.51848452600, 0.16613853300,  -0.026369431000};
+const double kA4b[7] = {0.026369431000, -0.16613853300, 0.51848452600, -1.27327473700,
+                        0.47476091400,  0.46884035700,  -0.049041958000};
+const double kA5[7] = {-0.20933762200, -1.08487567600, 2.14777605000, -1.38892832200,
+                       0.76894976600,  -0.28181465000, 0.048230454000};
+const double kA5b[7] = {-0.048230454000, 0.28181465000,  -0.76894976600, 1.38892832200,
+                        -2.14777605000,  1.08487567600, 0.20933762200};
+const double kA6[7] = {-2.19228033900, 4.74861140100, -5.10885191500, 4.46156710400,
+                       -2.83349874100, 1.12832886100, -0.20387637100};
+const double kA6b[7] = {0.20387637100, -1.12832886100, 2.83349874100, -4.46156710400,
+                        5.10885191500, -4.74861140100, 2.19228033900};
+const double kDf[7] = {0.190899511506,  -0.171503832236, 0.123632891797, -0.069975429105,
+                       0.029662754736, -0.008520738659, 0.001254597714};
+const double kDfbX[7] = {-0.057717512738, 0.199278374994,  -0.292668277650, 0.244537361546,
+                         -0.134605018019, 0.056184263460, -0.015009191593};
+const double kDfbY[7] = {(double)-0.057717512738f, (double)0.199278374994f,
+                         (double)-0.292668277650f, (double)0.244537361546f,
+                         (double)-0.134605018019f, (double)0.056184263460f,
+                         (double)-0.015009191593f};
+const double kAlpha[6] = {0.0, -0.737101392796, -1.634740794341,
+                          -0.744739003780, -1.469897351522, -2.813971388035};
+const double kBeta[6] = {0.032918605146, 0.823256998200, 0.381530948900,
+                         0.200092213184, 1.718581042715, 0.27};
+
+int berr(ns_batch *b, int code, const std::string &msg)
+{
+    if (b) b->err_text = msg;
+    ns::record_error(msg.c_str());
+    return code;
+}
+
+void coef_table(std::vector<double> &tab, int n, double h, const double *mesh, int D, int mode)
+{
+    tab.assign((size_t)n * ns::kCoefStride, 0.0);
+    for (int q = 0; q < n; q++) {
+        double mt = 1.0;
+        if (mode == NS_METRIC_EVERYWHERE || q < D || q >= n - D) mt = mesh[q];
+        double *c = &tab[(size_t)q * ns::kCoefStride];
+        const double *src = q == 0 ? kA6 : q == 1 ? kA5 : q == 2 ? kA4 : q == n - 3 ? kA4b
+                            : q == n - 2 ? kA5b : q == n - 1 ? kA6b : nullptr;
+        if (src)
+            for (int z = 0; z < 7; z++) c[z] = src[z] * mt / h;
+        else
+            for (int s = 0; s < 3; s++) c[4 + s] = kA[s] * mt / h;
+    }
+}
+
+void serial_filter(double *u, int n, double sigmaf, const double *dfb)
+{
+    for (int q = 1; q <= 6; q++) {
+        double Du = 0.0;
+        for (int s = -1; s <= 5; s++) Du += dfb[s + 1] * u[q + s];
+        u[q] -= sigmaf * Du;
+    }
+    for (int q = 6; q <= n - 7; q++) {
+        double Du = 0.0;
+        for (int s = -6; s <= 6; s++) Du += kDf[s < 0 ? -s : s] * u[q + s];
+        u[q] -= sigmaf * Du;
+    }
+    for (int q = n - 2; q >= n - 7; q--) {
+        double Du = 0.0;
+        for (int s = -1; s <= 5; s++) Du += dfb[s + 1] * u[q - s];
+        u[q] -= sigmaf * Du;
+    }
+}
+
+int warmup_len(double sigmaf, double thresh)
+{
+    const int kMax = 4096;
+    std::vector<double> e(kMax + 6);
+    int worst = 0;
+    for (int u = 0; u < 6; u++) {
+        std::fill(e.begin(), e.end(), 0.0);
+        e[u] = 1.0;
+        int last = 0;
+        for (int q = 6; q < kMax + 6; q++) {
+            double v = 0.0;
+            for (int s = 1; s <= 6; s++) v += -sigmaf * kDf[s] * e[q - s];
+            e[q] = v;
+            if (std::fabs(v) >= thresh) last = q - 5;
+        }
+        if (last >= kMax - 64) return -1;
+        worst = std::max(worst, last);
+    }
+    return std::max(worst + 8, 16);
+}
+
+double line_deriv(const double *f, int q, int n, const double *c)
+{
+    if (q >= 3 && q < n - 3)
+        return c[4] * (f[q + 1] - f[q - 1]) + c[5] * (f[q + 2] - f[q - 2]) + c[6] * (f[q + 3] - f[q - 3]);
+    const int o0 = (q < 3) ? -q : (n - 7 - q);
+    double r = 0.0;
+    for (int z = 0; z < 7; z++) r += c[z] * f[q + o0 + z];
+    return r;
+}
+
+template <class T>
+int balloc(ns_batch *b, T **p, size_t n)
+{
+    if (cudaMalloc((void **)p, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) {
+        *p = nullptr;
+        return berr(b, NS_ERR_OOM, "ns_batch: cudaMalloc failed");
+    }
+    return NS_OK;
+}
+
+// Allocates a device table of v in the state precision (es = 4: FP32, 8:
+// FP64) and uploads it synchronously.
+int tput(ns_batch *b, void **d, const std::vector<double> &v, size_t es)
+{
+    if (cudaMalloc(d, std::max<size_t>(v.size(), 1) * es) != cudaSuccess) {
+        *d = nullptr;
+        return berr(b, NS_ERR_OOM, "ns_batch: cudaMalloc failed");
+    }
+    cudaError_t e;
+    if (es == 4) {
+        std::vector<float> f(v.begin(), v.end());
+        e = cudaMemcpy(*d, f.data(), f.size() * 4, cudaMemcpyHostToDevice);
+    } else {
+        e = cudaMemcpy(*d, v.data(), v.size() * 8, cudaMemcpyHostToDevice);
+    }
+    if (e != cudaSuccess) return berr(b, NS_ERR_CUDA, "ns_batch: table upload failed");
+    return NS_OK;
+}
+
+template <class T>
+int bput(ns_batch *b, T *d, const std::vector<T> &v)
+{
+    if (v.empty()) return NS_OK;
+    if (cudaMemcpyAsync(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, b->stream) !=
+        cudaSuccess)
+        return berr(b, NS_ERR_CUDA, "ns_batch: upload failed");
+    return NS_OK;
+}
+
+void bfree(ns_batch *b)
+{
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    void *ps[] = {b->q[0], b->q[1], b->W, b->stage_sin, b->wf, b->dtv, b->drho, b->du,
+                  b->stagebuf, b->inst, b->tiles[0], b->tiles[1], b->fx, b->fy, b->bc,
+                  b->xc, b->xcl, b->yc, b->ycl, b->sigx, b->sigy, b->rho_bc, b->mrho, b->mu,
+                  b->mdrho, b->mdu, b->corr, b->src, b->bar, b->err, b->d_iter};
+    for (void *p : ps)
+        if (p) cudaFree(p);
+    if (b->own) cudaStreamDestroy(b->own);
+}
+
+template <typename T, int TY>
+cudaError_t launch_step_t(ns_batch *b, cudaStream_t s)
+{
+    ns::batch::Args a = b->args;
+    a.tiles = b->tiles[TY == 8 ? 0 : 1];
+    a.ntiles = b->ntiles[TY == 8 ? 0 : 1];
+    a.nblocks = (unsigned)b->grid;
+    void *kargs[] = {&a};
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)b->grid);
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = b->smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    (void)kargs;
+    return cudaLaunchKernelEx(&cfg, ns::batch::k_batch_step<T, TY>, a);
+}
+
+cudaError_t launch_step(ns_batch *b, cudaStream_t s)
+{
+    if (b->has_src) {
+        ns::batch::k_batch_sin<<<1, 256, 0, s>>>(b->wf, b->dtv, b->n, b->d_iter, b->stage_sin);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    if (b->precision == NS_PREC_SPLIT)
+        return b->ty == 8 ? launch_step_t<float, 8>(b, s) : launch_step_t<float, 16>(b, s);
+    return b->ty == 8 ? launch_step_t<double, 8>(b, s) : launch_step_t<double, 16>(b, s);
+}
+
+size_t smem_for(int precision, int ty)
+{
+    const size_t es = precision == NS_PREC_SPLIT ? 4 : 8;
+    const int pw = precision == NS_PREC_SPLIT ? 32 : 16;
+    const size_t tile = 4 * (size_t)(ty + 6) * 38 * es;
+    const size_t fx = (size_t)ns::batch::kWarps * 2 * 32 * (pw + 1) * es;
+    return std::max(tile, fx);
+}
+
+template <typename T, int TY>
+int occupancy(size_t smem)
+{
+    int nb = 0;
+    cudaFuncSetAttribute(ns::batch::k_batch_step<T, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, ns::batch::k_batch_step<T, TY>, 256, smem);
+    return nb;
+}
+
+int configure(ns_batch *b, int ty, int bps)
+{
+    int nsm = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, b->dev);
+    b->ty = ty;
+    b->smem = smem_for(b->precision, ty);
+    int maxb = b->precision == NS_PREC_SPLIT
+                   ? (ty == 8 ? occupancy<float, 8>(b->smem) : occupancy<float, 16>(b->smem))
+                   : (ty == 8 ? occupancy<double, 8>(b->smem) : occupancy<double, 16>(b->smem));
+    if (maxb < 1) return berr(b, NS_ERR_CUDA, "ns_batch: the step kernel cannot be resident");
+    b->blocks_per_sm = (bps > 0 && bps < maxb) ? bps : maxb;
+    b->grid = b->blocks_per_sm * nsm;
+    if (b->exec) {
+        cudaGraphExecDestroy(b->exec);
+        b->exec = nullptr;
+    }
+    return NS_OK;
+}
+
+int ensure_graph(ns_batch *b)
+{
+    if (b->exec) return NS_OK;
+    cudaStream_t cs;
+    if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess)
+        return berr(b, NS_ERR_CUDA, "ns_batch: stream");
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        cudaError_t le = launch_step(b, cs);
+        e = cudaStreamEndCapture(cs, &g);
+        if (le != cudaSuccess) e = le;
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, g, 0);
+    if (g) cudaGraphDestroy(g);
+    cudaStreamDestroy(cs);
+    if (e != cudaSuccess) {
+        b->exec = nullptr;
+        cudaGetLastError();
+        return berr(b, NS_ERR_CUDA, std::string("ns_batch: graph capture: ") + cudaGetErrorString(e));
+    }
+    return NS_OK;
+}
+
+int check_err(ns_batch *b)
+{
+    int h = 0;
+    if (cudaMemcpyAsync(&h, b->err, sizeof(int), cudaMemcpyDeviceToHost, b->stream) != cudaSuccess ||
+        cudaStreamSynchronize(b->stream) != cudaSuccess)
+        return berr(b, NS_ERR_CUDA, std::string("ns_batch: ") + cudaGetErrorString(cudaGetLastError()));
+    if (h) {
+        cudaMemsetAsync(b->err, 0, sizeof(int), b->stream);
+        cudaMemsetAsync(b->bar, 0, 2 * sizeof(unsigned), b->stream);
+        cudaStreamSynchronize(b->stream);
+        return berr(b, NS_ERR_TIMEOUT, "ns_batch: a phase barrier of the persistent step kernel timed out");
+    }
+    return NS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ns_batch_create(const ns_params *const *params, int n, int precision, ns_batch **out)
+{
+    if (!out || !params || n < 1) return berr(nullptr, NS_ERR_PARAM, "ns_batch_create: bad argument");
+    *out = nullptr;
+    if (precision != NS_PREC_FP64 && precision != NS_PREC_SPLIT)
+        return berr(nullptr, NS_ERR_PARAM, "ns_batch_create: precision");
+    for (int q = 0; q < n; q++) {
+        const ns_params *p = params[q];
+        if (!p || p->abi_version != NS_ABI_VERSION || !p->inviscid || p->nk != 4 || p->imax < 13 ||
+            p->jmax < 13 || p->D < 0 || 2 * p->D > p->imax || 2 * p->D > p->jmax ||
+            !(p->dt > 0) || !(p->dm > 0) || !(p->dn > 0) || !p->meshx || !p->meshy ||
+            !p->sigmax || !p->sigmay || !p->rhob || !p->Ub ||
+            (p->source_mode == NS_SRC_GAUSSIAN && (!p->m || !p->n || !(p->r0 != 0.0))) ||
+            (p->source_mode == NS_SRC_FIELD && !p->src_field) || p->device != params[0]->device ||
+            p->sigmaf != params[0]->sigmaf)
+            return berr(nullptr, NS_ERR_PARAM,
+                        "ns_batch_create: instance " + std::to_string(q) +
+                            ": each instance must be a valid Euler case (inviscid=1, nk=4) on "
+                            "the same device with the same sigmaf");
+    }
+    ns_batch *b = new (std::nothrow) ns_batch();
+    if (!b) return berr(nullptr, NS_ERR_OOM, "ns_batch_create: host allocation");
+    b->n = n;
+    b->dev = params[0]->device;
+    b->precision = precision;
+    int rc = NS_OK;
+    const size_t es = precision == NS_PREC_SPLIT ? 4 : 8;
+    std::vector<ns::batch::Inst> hin(n);
+    std::vector<double> xcd, ycd;
+    std::vector<double> xc, yc, sx, sy, rbc, mrho, mu, mdrho, mdu, corr;
+    std::vector<float> xcl, ycl;
+    std::vector<double> rhoj, uj, wfv, dtv;
+    long long qoff = 0, woff = 0, soff = 0;
+    int xoff = 0, yoff = 0;
+    double sigmaf = params[0]->sigmaf;
+    const int warm = warmup_len(sigmaf, precision == NS_PREC_SPLIT ? std::ldexp(1.0, -32)
+                                                                   : std::ldexp(1.0, -60));
+    for (int q = 0; q < n && rc == NS_OK; q++) {
+        const ns_params *p = params[q];
+        const int imax = p->imax, jmax = p->jmax;
+        auto ub = [&](int k, int i, int j) -> double {
+            return p->ub_layout == NS_LAYOUT_FORTRAN ? p->Ub[k + 4 * ((size_t)i + (size_t)imax * j)]
+                                                     : p->Ub[((size_t)k * jmax + j) * imax + i];
+        };
+        const double pb = ub(3, 0, 0);
+        std::vector<double> rj(jmax), uj2(jmax);
+        for (int j = 0; j < jmax; j++) {
+            rj[j] = ub(0, 0, j);
+            uj2[j] = ub(1, 0, j);
+            for (int i = 0; i < imax; i++)
+                if (ub(0, i, j) != rj[j] || ub(1, i, j) != uj2[j] || ub(2, i, j) != 0.0 || ub(3, i, j) != pb)
+                    rc = berr(b, NS_ERR_UNSUPPORTED,
+                              "ns_batch_create: instance " + std::to_string(q) +
+                                  ": the base flow must be uniform in x with v = 0 and uniform p");
+        }
+        if (rc != NS_OK) break;
+        ns::batch::Inst &in = hin[q];
+        in.imax = imax;
+        in.jmax = jmax;
+        in.D = p->D;
+        in.pitch = (imax + 31) / 32 * 32;
+        in.q_off = qoff;
+        in.w_off = woff;
+        qoff += 4LL * in.pitch * jmax;
+        woff += 4LL * in.pitch * jmax;
+        in.x_off = xoff;
+        in.y_off = yoff;
+        in.dt_d = p->dt;
+        in.pmean_d = pb;
+        in.gamma_d = p->gamma;
+        in.p_bc_d = 1.0 / p->gamma - pb;
+        in.dt_f = (float)in.dt_d;
+        in.pmean_f = (float)in.pmean_d;
+        in.gamma_f = (float)in.gamma_d;
+        in.p_bc_f = (float)in.p_bc_d;
+        in.warm = warm;
+        if (p->source_mode != NS_SRC_NONE) {
+            in.s_off = soff;
+            soff += (long long)in.pitch * jmax;
+            b->has_src = true;
+        } else {
+            in.s_off = -1;
+        }
+        // chunks: items of roughly 256 positions
+        auto nchunks = [&](int nn) {
+            if (warm < 0) return 1;
+            int c = (nn - 12) / 256;
+            const int maxc = (nn - 12) / (4 * (warm + 6));
+            c = std::min(c, maxc);
+            return std::max(c, 1);
+        };
+        in.fx_chunks = nchunks(imax);
+        in.fy_chunks = nchunks(jmax);
+        coef_table(xcd, imax, p->dm, p->meshx, p->D, p->metric_mode);
+        coef_table(ycd, jmax, p->dn, p->meshy, p->D, p->metric_mode);
+        for (double v : xcd) {
+            xc.push_back(v);
+            xcl.push_back((float)(v - (double)(float)v));
+        }
+        for (double v : ycd) {
+            yc.push_back(v);
+            ycl.push_back((float)(v - (double)(float)v));
+        }
+        for (int i = 0; i < imax; i++) sx.push_back(p->sigmax[i]);
+        for (int j = 0; j < jmax; j++) {
+            sy.push_back(p->sigmay[j]);
+            rbc.push_back(p->rhob[j] - rj[j]);
+            mrho.push_back(rj[j]);
+            mu.push_back(uj2[j]);
+            mdrho.push_back(line_deriv(rj.data(), j, jmax, &ycd[(size_t)j * ns::kCoefStride]));
+            mdu.push_back(line_deriv(uj2.data(), j, jmax, &ycd[(size_t)j * ns::kCoefStride]));
+            rhoj.push_back(rj[j]);
+            uj.push_back(uj2[j]);
+        }
+        std::vector<double> col(jmax), f(jmax);
+        for (int k = 0; k < 4; k++) {
+            for (int j = 0; j < jmax; j++) col[j] = k == 0 ? rj[j] : k == 1 ? uj2[j] : k == 2 ? 0.0 : pb;
+            f = col;
+            serial_filter(f.data(), jmax, sigmaf, kDfbY);
+            for (int j = 0; j < jmax; j++) corr.push_back(f[j] - col[j]);
+        }
+        b->hpmean.push_back(pb);
+        wfv.push_back(p->wf);
+        dtv.push_back(p->dt);
+        xoff += imax;
+        yoff += jmax;
+    }
+    if (rc != NS_OK) {
+        delete b;
+        return rc;
+    }
+    b->hinst = hin;
+    b->hrho = rhoj;
+    b->hu = uj;
+    b->qsize = (size_t)qoff;
+    b->wsize = (size_t)woff;
+    if (cudaSetDevice(b->dev) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&b->own, cudaStreamNonBlocking) != cudaSuccess) {
+        delete b;
+        return berr(nullptr, NS_ERR_CUDA, "ns_batch_create: device or stream");
+    }
+    b->stream = b->own;
+    // work lists
+    std::vector<int4> tiles8, tiles16, fxl, fyl;
+    std::vector<int> bcl;
+    for (int q = 0; q < n; q++) {
+        const auto &in = hin[q];
+        for (int j0 = 0; j0 < in.jmax; j0 += 8)
+            for (int i0 = 0; i0 < in.imax; i0 += 32) tiles8.push_back(make_int4(q, i0, j0, 0));
+        for (int j0 = 0; j0 < in.jmax; j0 += 16)
+            for (int i0 = 0; i0 < in.imax; i0 += 32) tiles16.push_back(make_int4(q, i0, j0, 0));
+        for (int k = 0; k < 4; k++) {
+            for (int r0 = 0; r0 < in.jmax; r0 += 32)
+                for (int c = 0; c < in.fx_chunks; c++) fxl.push_back(make_int4(q, k, r0, c));
+            for (int c0 = 0; c0 < in.imax; c0 += 32)
+                for (int c = 0; c < in.fy_chunks; c++) fyl.push_back(make_int4(q, k, c0, c));
+        }
+        bcl.push_back(q);
+    }
+    b->ntiles[0] = (int)tiles8.size();
+    b->ntiles[1] = (int)tiles16.size();
+    b->nfx = (int)fxl.size();
+    b->nfy = (int)fyl.size();
+    b->nbc = (int)bcl.size();
+    size_t maxplane = 0;
+    for (const auto &in : hin) maxplane = std::max(maxplane, (size_t)in.pitch * in.jmax);
+    b->stagebuf_elems = 8 * maxplane;
+#define B_TRY(x)                  \
+    do {                          \
+        rc = (x);                 \
+        if (rc != NS_OK) goto fail; \
+    } while (0)
+    B_TRY(balloc(b, (unsigned char **)&b->q[0], b->qsize * es));
+    B_TRY(balloc(b, (unsigned char **)&b->q[1], b->qsize * es));
+    B_TRY(balloc(b, &b->W, b->wsize));
+    B_TRY(balloc(b, &b->stage_sin, (size_t)8 * n));
+    B_TRY(balloc(b, &b->wf, (size_t)n));
+    B_TRY(balloc(b, &b->dtv, (size_t)n));
+    B_TRY(balloc(b, &b->drho, rhoj.size()));
+    B_TRY(balloc(b, &b->du, uj.size()));
+    B_TRY(balloc(b, &b->stagebuf, b->stagebuf_elems));
+    B_TRY(balloc(b, &b->inst, (size_t)n));
+    B_TRY(balloc(b, &b->tiles[0], tiles8.size()));
+    B_TRY(balloc(b, &b->tiles[1], tiles16.size()));
+    B_TRY(balloc(b, &b->fx, fxl.size()));
+    B_TRY(balloc(b, &b->fy, fyl.size()));
+    B_TRY(balloc(b, &b->bc, bcl.size()));
+    B_TRY(balloc(b, &b->xcl, xcl.size()));
+    B_TRY(balloc(b, &b->ycl, ycl.size()));
+    B_TRY(tput(b, &b->xc, xc, es));
+    B_TRY(tput(b, &b->yc, yc, es));
+    B_TRY(tput(b, &b->sigx, sx, es));
+    B_TRY(tput(b, &b->sigy, sy, es));
+    B_TRY(tput(b, &b->rho_bc, rbc, es));
+    B_TRY(tput(b, &b->mrho, mrho, es));
+    B_TRY(tput(b, &b->mu, mu, es));
+    B_TRY(tput(b, &b->mdrho, mdrho, es));
+    B_TRY(tput(b, &b->mdu, mdu, es));
+    B_TRY(tput(b, &b->corr, corr, es));
+    B_TRY(balloc(b, (unsigned char **)&b->src, std::max<long long>(soff, 1) * es));
+    B_TRY(balloc(b, &b->bar, 2));
+    B_TRY(balloc(b, &b->err, 1));
+    B_TRY(balloc(b, &b->d_iter, 1));
+    if (cudaMemsetAsync(b->q[0], 0, b->qsize * es, b->stream) != cudaSuccess ||
+        cudaMemsetAsync(b->q[1], 0, b->qsize * es, b->stream) != cudaSuccess ||
+        cudaMemsetAsync(b->W, 0, b->wsize * 8, b->stream) != cudaSuccess ||
+        cudaMemsetAsync(b->stage_sin, 0, 8 * n * sizeof(double), b->stream) != cudaSuccess ||
+        cudaMemsetAsync(b->bar, 0, 2 * sizeof(unsigned), b->stream) != cudaSuccess ||
+        cudaMemsetAsync(b->err, 0, sizeof(int), b->stream) != cudaSuccess ||
+        cudaMemsetAsync(b->d_iter, 0, sizeof(int), b->stream) != cudaSuccess) {
+        rc = berr(b, NS_ERR_CUDA, "ns_batch_create: memset");
+        goto fail;
+    }
+    B_TRY(bput(b, b->inst, hin));
+    B_TRY(bput(b, b->tiles[0], tiles8));
+    B_TRY(bput(b, b->tiles[1], tiles16));
+    B_TRY(bput(b, b->fx, fxl));
+    B_TRY(bput(b, b->fy, fyl));
+    B_TRY(bput(b, b->bc, bcl));
+    B_TRY(bput(b, b->xcl, xcl));
+    B_TRY(bput(b, b->ycl, ycl));
+    B_TRY(bput(b, b->drho, rhoj));
+    B_TRY(bput(b, b->du, uj));
+    B_TRY(bput(b, b->wf, wfv));
+    B_TRY(bput(b, b->dtv, dtv));
+    if (b->has_src) {
+        // spatial source fields (rk.f90:188-189), in the state's precision
+        for (int q = 0; q < n; q++) {
+            const ns_params *p = params[q];
+            const auto &in = hin[q];
+            if (in.s_off < 0) continue;
+            std::vector<double> fld((size_t)in.pitch * in.jmax, 0.0);
+            for (int j = 0; j < in.jmax; j++)
+                for (int i = 0; i < in.imax; i++) {
+                    double v;
+                    if (p->source_mode == NS_SRC_GAUSSIAN) {
+                        const double dx = p->m[i] - p->m_pt, dy = p->n[j] - p->n_pt;
+                        v = p->amplitude * std::exp(-(std::log(2.0) * (dx * dx + dy * dy) / (p->r0 * p->r0)));
+                    } else {
+                        v = p->src_field[(size_t)j * in.imax + i];
+                    }
+                    fld[(size_t)j * in.pitch + i] = v;
+                }
+            cudaError_t e;
+            if (precision == NS_PREC_SPLIT) {
+                std::vector<float> ff(fld.begin(), fld.end());
+                e = cudaMemcpy((float *)b->src + in.s_off, ff.data(), ff.size() * 4, cudaMemcpyHostToDevice);
+            } else {
+                e = cudaMemcpy((double *)b->src + in.s_off, fld.data(), fld.size() * 8, cudaMemcpyHostToDevice);
+            }
+            if (e != cudaSuccess) {
+                rc = berr(b, NS_ERR_CUDA, "ns_batch_create: source upload");
+                goto fail;
+            }
+        }
+    }
+    if (cudaStreamSynchronize(b->stream) != cudaSuccess) {
+        rc = berr(b, NS_ERR_CUDA, "ns_batch_create: setup");
+        goto fail;
+    }
+    {
+        ns::batch::Args &a = b->args;
+        a.inst = b->inst;
+        a.fx = b->fx;
+        a.fy = b->fy;
+        a.bc = b->bc;
+        a.nfx = b->nfx;
+        a.nfy = b->nfy;
+        a.nbc = b->nbc;
+        a.q0 = b->q[0];
+        a.q1 = b->q[1];
+        a.W = b->W;
+        a.xc = b->xc; a.xcl = b->xcl; a.yc = b->yc; a.ycl = b->ycl;
+        a.sigx = b->sigx; a.sigy = b->sigy; a.rho_bc = b->rho_bc;
+        a.mrho = b->mrho; a.mu = b->mu; a.mdrho = b->mdrho; a.mdu = b->mdu; a.corr = b->corr;
+        a.src = b->src;
+        a.stage_sin = b->stage_sin;
+        for (int k = 0; k < 6; k++) {
+            a.alpha[k] = kAlpha[k];
+            a.beta[k] = kBeta[k];
+        }
+        a.fm_d[0] = 0.0;
+        for (int s = 1; s <= 6; s++) a.fm_d[s] = -sigmaf * kDf[s];
+        const double *dfb[2] = {kDfbX, kDfbY};
+        for (int d = 0; d < 2; d++) {
+            a.fbm1_d[d] = -sigmaf * dfb[d][0];
+            double sum = 0.0;
+            for (int z = 0; z < 7; z++) sum += dfb[d][z];
+            a.fbsum_d[d] = -sigmaf * sum;
+            a.fb_d[d][0] = 0.0;
+            for (int z = 1; z <= 5; z++) a.fb_d[d][z] = -sigmaf * dfb[d][z + 1];
+        }
+        for (int s = 0; s < 7; s++) a.fm_f[s] = (float)a.fm_d[s];
+        for (int d = 0; d < 2; d++) {
+            a.fbm1_f[d] = (float)a.fbm1_d[d];
+            a.fbsum_f[d] = (float)a.fbsum_d[d];
+            for (int z = 0; z < 6; z++) a.fb_f[d][z] = (float)a.fb_d[d][z];
+        }
+        a.bar_count = b->bar;
+        a.bar_gen = b->bar + 1;
+        a.err = b->err;
+        a.spin_limit = 20000000;  // x 64 ns sleeps: about 1-2 s per barrier
+    }
+    rc = configure(b, 16, 0);
+    if (rc != NS_OK) goto fail;
+#undef B_TRY
+    *out = b;
+    return NS_OK;
+fail:
+    bfree(b);
+    delete b;
+    return rc;
+}
+
+void ns_batch_destroy(ns_batch *b)
+{
+    if (!b) return;
+    cudaSetDevice(b->dev);
+    cudaStreamSynchronize(b->stream);
+    bfree(b);
+    delete b;
+}
+
+// Host state of instance q (layout as ns_set_state) -> q' (FP32 or FP64).
+int ns_batch_set_state(ns_batch *b, int q, const double *U, int layout)
+{
+    if (!b || !U || q < 0 || q >= b->n) return berr(b, NS_ERR_PARAM, "ns_batch_set_state: bad argument");
+    cudaSetDevice(b->dev);
+    const auto &in = b->hinst[q];
+    const size_t row = (size_t)in.imax * 8;
+    double *stg = b->stagebuf;                 // 4 FP64 planes with pitch in.pitch
+    double *raw = b->stagebuf + 4 * (size_t)in.pitch * in.jmax;
+    cudaError_t e;
+    ns::Dims d;
+    d.imax = in.imax;
+    d.jmax = in.jmax;
+    d.pitch = in.pitch;
+    d.nk = 4;
+    d.D = in.D;
+    d.plane = (long long)in.pitch * in.jmax;
+    if (layout == NS_LAYOUT_SOA) {
+        e = cudaMemcpy2DAsync(stg, in.pitch * 8, U, row, row, (size_t)in.jmax * 4,
+                              cudaMemcpyHostToDevice, b->stream);
+    } else if (layout == NS_LAYOUT_FORTRAN) {
+        e = cudaMemcpyAsync(raw, U, (size_t)4 * in.imax * in.jmax * 8, cudaMemcpyHostToDevice, b->stream);
+        if (e == cudaSuccess) e = ns::launch_aos_to_soa(raw, stg, d, b->stream);
+    } else {
+        return berr(b, NS_ERR_PARAM, "ns_batch_set_state: layout");
+    }
+    const dim3 blk(32, 8), grd((in.imax + 31) / 32, (in.jmax + 7) / 8);
+    if (e == cudaSuccess) {
+        if (b->precision == NS_PREC_SPLIT)
+            ns::batch::k_batch_from_full<float><<<grd, blk, 0, b->stream>>>(
+                stg, in.imax, in.jmax, in.pitch, b->drho + in.y_off, b->du + in.y_off,
+                b->hpmean[q], (float *)b->q[0] + in.q_off, in.pitch);
+        else
+            ns::batch::k_batch_from_full<double><<<grd, blk, 0, b->stream>>>(
+                stg, in.imax, in.jmax, in.pitch, b->drho + in.y_off, b->du + in.y_off,
+                b->hpmean[q], (double *)b->q[0] + in.q_off, in.pitch);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    if (e != cudaSuccess) return berr(b, NS_ERR_CUDA, std::string("ns_batch_set_state: ") + cudaGetErrorString(e));
+    b->have_state = true;
+    return NS_OK;
+}
+
+int ns_batch_get_state(ns_batch *b, int q, double *U, int layout)
+{
+    if (!b || !U || q < 0 || q >= b->n) return berr(b, NS_ERR_PARAM, "ns_batch_get_state: bad argument");
+    cudaSetDevice(b->dev);
+    const auto &in = b->hinst[q];
+    const size_t row = (size_t)in.imax * 8;
+    double *stg = b->stagebuf;
+    double *raw = b->stagebuf + 4 * (size_t)in.pitch * in.jmax;
+    const dim3 blk(32, 8), grd((in.imax + 31) / 32, (in.jmax + 7) / 8);
+    if (b->precision == NS_PREC_SPLIT)
+        ns::batch::k_batch_to_full<float><<<grd, blk, 0, b->stream>>>(
+            (float *)b->q[0] + in.q_off, in.imax, in.jmax, in.pitch, b->drho + in.y_off,
+            b->du + in.y_off, b->hpmean[q], stg, in.pitch);
+    else
+        ns::batch::k_batch_to_full<double><<<grd, blk, 0, b->stream>>>(
+            (double *)b->q[0] + in.q_off, in.imax, in.jmax, in.pitch, b->drho + in.y_off,
+            b->du + in.y_off, b->hpmean[q], stg, in.pitch);
+    cudaError_t e = cudaGetLastError();
+    ns::Dims d;
+    d.imax = in.imax;
+    d.jmax = in.jmax;
+    d.pitch = in.pitch;
+    d.nk = 4;
+    d.D = in.D;
+    d.plane = (long long)in.pitch * in.jmax;
+    if (e == cudaSuccess) {
+        if (layout == NS_LAYOUT_SOA) {
+            e = cudaMemcpy2DAsync(U, row, stg, in.pitch * 8, row, (size_t)in.jmax * 4,
+                                  cudaMemcpyDeviceToHost, b->stream);
+        } else if (layout == NS_LAYOUT_FORTRAN) {
+            e = ns::launch_soa_to_aos(stg, raw, d, b->stream);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(U, raw, (size_t)4 * in.imax * in.jmax * 8, cudaMemcpyDeviceToHost, b->stream);
+        } else {
+            return berr(b, NS_ERR_PARAM, "ns_batch_get_state: layout");
+        }
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    if (e != cudaSuccess) return berr(b, NS_ERR_CUDA, std::string("ns_batch_get_state: ") + cudaGetErrorString(e));
+    return NS_OK;
+}
+
+int ns_batch_step(ns_batch *b, int iter0, int nsteps)
+{
+    if (!b || nsteps < 0) return berr(b, NS_ERR_PARAM, "ns_batch_step: bad argument");
+    if (!b->have_state) return berr(b, NS_ERR_STATE, "ns_batch_step before ns_batch_set_state");
+    cudaSetDevice(b->dev);
+    if (!b->no_graph && ensure_graph(b) != NS_OK) b->no_graph = true;  // launch directly
+    if (b->has_src) ns::batch::k_batch_set_iter<<<1, 1, 0, b->stream>>>(b->d_iter, iter0);
+    for (int s = 0; s < nsteps; s++) {
+        const cudaError_t e = b->no_graph ? launch_step(b, b->stream)
+                                          : cudaGraphLaunch(b->exec, b->stream);
+        if (e != cudaSuccess)
+            return berr(b, NS_ERR_CUDA, std::string("ns_batch_step: ") + cudaGetErrorString(e));
+    }
+    return NS_OK;
+}
+
+int ns_batch_synchronize(ns_batch *b)
+{
+    if (!b) return berr(nullptr, NS_ERR_PARAM, "ns_batch_synchronize: NULL");
+    cudaSetDevice(b->dev);
+    if (cudaStreamSynchronize(b->stream) != cudaSuccess)
+        return berr(b, NS_ERR_CUDA, std::string("ns_batch_synchronize: ") + cudaGetErrorString(cudaGetLastError()));
+    return check_err(b);
+}
+
+int ns_batch_set_stream(ns_batch *b, void *stream)
+{
+    if (!b) return berr(nullptr, NS_ERR_PARAM, "ns_batch_set_stream: NULL");
+    b->stream = stream ? (cudaStream_t)stream : b->own;
+    return NS_OK;
+}
+
+// Tile autotuner: times each tile height (8, 16 rows) and residency (1 block
+// per SM up to the maximum) for `reps` steps on the current state, keeps the
+// fastest, and leaves the state advanced by the steps it ran.
+int ns_batch_autotune(ns_batch *b, int iter0, int reps, int *ty, int *blocks_per_sm, double *ms)
+{
+    if (!b || reps < 1) return berr(b, NS_ERR_PARAM, "ns_batch_autotune: bad argument");
+    if (!b->have_state) return berr(b, NS_ERR_STATE, "ns_batch_autotune before ns_batch_set_state");
+    cudaSetDevice(b->dev);
+    double best = 1e300;
+    int bty = 16, bbps = 0;
+    int it = iter0;
+    for (int t : {8, 16}) {
+        const size_t sm = smem_for(b->precision, t);
+        const int maxb = b->precision == NS_PREC_SPLIT
+                             ? (t == 8 ? occupancy<float, 8>(sm) : occupancy<float, 16>(sm))
+                             : (t == 8 ? occupancy<double, 8>(sm) : occupancy<double, 16>(sm));
+        for (int bps = 1; bps <= maxb; bps++) {
+            int rc = configure(b, t, bps);
+            if (rc != NS_OK) return rc;
+            if (!b->no_graph && ensure_graph(b) != NS_OK) b->no_graph = true;
+            auto one = [&]() {
+                return b->no_graph ? launch_step(b, b->stream) : cudaGraphLaunch(b->exec, b->stream);
+            };
+            if (b->has_src) ns::batch::k_batch_set_iter<<<1, 1, 0, b->stream>>>(b->d_iter, it);
+            one();  // warm-up
+            cudaEvent_t e0, e1;
+            cudaEventCreate(&e0);
+            cudaEventCreate(&e1);
+            cudaEventRecord(e0, b->stream);
+            for (int r = 0; r < reps; r++) one();
+            cudaEventRecord(e1, b->stream);
+            cudaEventSynchronize(e1);
+            float t_ms = 0.f;
+            cudaEventElapsedTime(&t_ms, e0, e1);
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            it += reps + 1;
+            rc = check_err(b);
+            if (rc != NS_OK) return rc;
+            if (t_ms / reps < best) {
+                best = t_ms / reps;
+                bty = t;
+                bbps = bps;
+            }
+        }
+    }
+    int rc = configure(b, bty, bbps);
+    if (rc != NS_OK) return rc;
+    b->tuned_ms = best;
+    if (ty) *ty = bty;
+    if (blocks_per_sm) *blocks_per_sm = b->blocks_per_sm;
+    if (ms) *ms = best;
+    return NS_OK;
+}
+
+// Test hook for the bounded barrier: the next step waits for `extra` blocks
+// that never come, with a spin limit of `spin_limit`; the step must then
+// return NS_ERR_TIMEOUT from ns_batch_synchronize and leave the context usable.
+int ns_batch_barrier_test(ns_batch *b, int extra, long long spin_limit)
+{
+    if (!b || extra < 0 || spin_limit < 1) return berr(b, NS_ERR_PARAM, "ns_batch_barrier_test: bad argument");
+    cudaSetDevice(b->dev);
+    ns::batch::Args saved = b->args;
+    b->args.spin_limit = spin_limit;
+    const int g = b->grid;
+    b->grid = g;
+    // launch directly (no graph) with a participant count that cannot be met
+    ns::batch::Args a = b->args;
+    a.tiles = b->tiles[b->ty == 8 ? 0 : 1];
+    a.ntiles = b->ntiles[b->ty == 8 ? 0 : 1];
+    a.nblocks = (unsigned)(g + extra);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)g);
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = b->smem;
+    cfg.stream = b->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaError_t e;
+    if (b->precision == NS_PREC_SPLIT)
+        e = b->ty == 8 ? cudaLaunchKernelEx(&cfg, ns::batch::k_batch_step<float, 8>, a)
+                       : cudaLaunchKernelEx(&cfg, ns::batch::k_batch_step<float, 16>, a);
+    else
+        e = b->ty == 8 ? cudaLaunchKernelEx(&cfg, ns::batch::k_batch_step<double, 8>, a)
+                       : cudaLaunchKernelEx(&cfg, ns::batch::k_batch_step<double, 16>, a);
+    b->args = saved;
+    if (e != cudaSuccess) return berr(b, NS_ERR_CUDA, std::string("ns_batch_barrier_test: ") + cudaGetErrorString(e));
+    return ns_batch_synchronize(b);
+}
+
+int ns_batch_info(ns_batch *b, int *grid, int *ty, int *blocks_per_sm, int *items)
+{
+    if (!b) return berr(nullptr, NS_ERR_PARAM, "ns_batch_info: NULL");
+    if (grid) *grid = b->grid;
+    if (ty) *ty = b->ty;
+    if (blocks_per_sm) *blocks_per_sm = b->blocks_per_sm;
+    if (items) {
+        items[0] = b->ntiles[b->ty == 8 ? 0 : 1];
+        items[1] = b->nfx;
+        items[2] = b->nfy;
+        items[3] = b->nbc;
+    }
+    return NS_OK;
+}
+
+}  // extern "C"

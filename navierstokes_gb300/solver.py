@@ -120,3 +120,82 @@ class Solver:
 
     def set_stream(self, stream_handle: int) -> None:
         self._rc(self.lib.ns_set_stream(self._ctx, C.c_void_p(stream_handle)))
+
+
+class Batch:
+    """Many independent Euler instances advanced together (ns_batch_*)."""
+
+    def __init__(self, case_list, device: int = 0, precision: int = L.NS_PREC_FP64):
+        self.lib = L.load()
+        self.cases = list(case_list)
+        self._keep = []
+        ps = []
+        for c in self.cases:
+            p, keep = params_from_case(c, device=device, precision=precision)
+            self._keep.append((p, keep))
+            ps.append(p)
+        arr = (C.c_void_p * len(ps))(*[C.addressof(p) for p in ps])
+        h = C.c_void_p()
+        L.check(self.lib.ns_batch_create(arr, len(ps), int(precision), C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.lib.ns_batch_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _rc(self, rc):
+        L.check(rc)
+
+    def set_state(self, q: int, U: np.ndarray) -> None:
+        c = self.cases[q]
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        assert U.shape == (c.jmax, c.imax, 4)
+        self._rc(self.lib.ns_batch_set_state(self._h, q, U.ctypes.data, L.NS_LAYOUT_FORTRAN))
+
+    def get_state(self, q: int) -> np.ndarray:
+        c = self.cases[q]
+        out = np.empty((c.jmax, c.imax, 4))
+        self._rc(self.lib.ns_batch_get_state(self._h, q, out.ctypes.data, L.NS_LAYOUT_FORTRAN))
+        return out
+
+    def set_initial(self) -> None:
+        for q, c in enumerate(self.cases):
+            self.set_state(q, c.U0)
+
+    def step(self, iter0: int, nsteps: int = 1) -> None:
+        self._rc(self.lib.ns_batch_step(self._h, int(iter0), int(nsteps)))
+
+    def synchronize(self) -> None:
+        self._rc(self.lib.ns_batch_synchronize(self._h))
+
+    def set_stream(self, handle: int) -> None:
+        self._rc(self.lib.ns_batch_set_stream(self._h, C.c_void_p(handle)))
+
+    def autotune(self, iter0: int = 0, reps: int = 2):
+        ty, bps, ms = C.c_int(), C.c_int(), C.c_double()
+        self._rc(self.lib.ns_batch_autotune(self._h, iter0, reps, C.byref(ty), C.byref(bps),
+                                            C.byref(ms)))
+        return ty.value, bps.value, ms.value
+
+    def info(self):
+        g, ty, bps = C.c_int(), C.c_int(), C.c_int()
+        items = (C.c_int * 4)()
+        self._rc(self.lib.ns_batch_info(self._h, C.byref(g), C.byref(ty), C.byref(bps), items))
+        return {"grid": g.value, "tile_rows": ty.value, "blocks_per_sm": bps.value,
+                "items": list(items)}
+
+    def barrier_test(self, extra: int = 1, spin_limit: int = 20000) -> int:
+        return self.lib.ns_batch_barrier_test(self._h, extra, spin_limit)
