@@ -293,6 +293,55 @@ def split_study(args, local, hbm_peak):
     return out
 
 
+def batch_study(args, local):
+    """Config-4 workload: 64 independent Euler instances, sizes log-uniform in
+    [128, 1024] (multiples of 32), monopole sources, mean flow M ~ U[0, 0.6],
+    numpy.random.default_rng(0); 300 steps in one persistent launch per step,
+    FP64 and split precision, tiles autotuned."""
+    import torch
+    from navierstokes_gb300 import Batch, cases
+    from navierstokes_gb300 import _lib as L
+    cs = cases.sweep_cases(n=args.batch_n, seed=0)
+    pts = sum(c.points for c in cs)
+    out = {"workload": f"{len(cs)} Euler instances, Nx,Ny in [128,1024] log-uniform (seed 0), "
+                       f"{pts} points in total, monopole sources, M ~ U[0,0.6], "
+                       f"{args.batch_steps} steps", "points": pts}
+    finals = {}
+    for name, prec in (("fp64", L.NS_PREC_FP64), ("split", L.NS_PREC_SPLIT)):
+        b = Batch(cs, device=local, precision=prec)
+        stream = torch.cuda.Stream()
+        b.set_stream(stream.cuda_stream)
+        b.set_initial()
+        ty, bps, tms = b.autotune(0, 2)
+        b.set_initial()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b.step(0, args.batch_steps)
+        e1.record(stream)
+        b.synchronize()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.batch_steps
+        finals[name] = [b.get_state(q) for q in range(len(cs))]
+        out[name] = {"value": pts / (ms * 1e-3) / 1e6, "unit": UNIT, "ms_per_step": ms,
+                     "tile_rows": ty, "blocks_per_sm": bps, "launch": b.info()}
+        b.close()
+    l2n = l2d = 0.0
+    mx = mref = 0.0
+    for q, c in enumerate(cs):
+        dp = finals["split"][q][..., 3] - finals["fp64"][q][..., 3]
+        pr = finals["fp64"][q][..., 3] - c.Ub[..., 3]
+        l2n += float(np.sum(dp * dp))
+        l2d += float(np.sum(pr * pr))
+        mx = max(mx, float(np.max(np.abs(dp))))
+        mref = max(mref, float(np.max(np.abs(pr))))
+    out["split_speedup_vs_fp64"] = out["split"]["value"] / out["fp64"]["value"]
+    out["split_p_error_vs_fp64"] = {"p_rel_l2": (l2n / l2d) ** 0.5, "p_rel_max": mx / mref,
+                                    "at_step": args.batch_steps}
+    return out
+
+
 def cpu_baseline_sample(case, seconds=20.0):
     """Oracle on the host cores, a bounded sample of the same workload."""
     import oracle
@@ -433,6 +482,13 @@ def run_ours(args, world, rank, local, pg):
         except Exception as e:
             split = {"failed": str(e)}
 
+    batched = None
+    if rank == 0 and world == 1 and not args.no_batch:
+        try:
+            batched = batch_study(args, local)
+        except Exception as e:
+            batched = {"failed": str(e)}
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
@@ -458,6 +514,8 @@ def run_ours(args, world, rank, local, pg):
             line["cpu_baseline"] = cpu
         if split is not None:
             line["split_precision"] = split
+        if batched is not None:
+            line["batched"] = batched
         print(json.dumps(line), flush=True)
 
 
@@ -474,6 +532,10 @@ def main():
     ap.add_argument("--no-split", action="store_true",
                     help="skip the split-precision (config-3) study")
     ap.add_argument("--split-n", type=int, default=4096)
+    ap.add_argument("--no-batch", action="store_true",
+                    help="skip the batched-sweep (config-4) study")
+    ap.add_argument("--batch-n", type=int, default=64)
+    ap.add_argument("--batch-steps", type=int, default=300)
     ap.add_argument("--split-error-steps", type=lambda t: [int(x) for x in t.split(",")],
                     default=[100, 500, 1000])
     args = ap.parse_args()

@@ -211,12 +211,10 @@ __device__ void stage_tile(const Args &a, int st, int4 item, const T *qin, T *qo
                 } else {
                     const int o0 = (i < 3) ? -i : (in.imax - 7 - i);
                     const T *g = q + k * plane + idx + o0;
-                    const T f0 = q[k * plane + idx];
+                    const T f0 = (sizeof(T) == 4) ? q[k * plane + idx] : T(0);
                     T r = T(0);
 #pragma unroll
-                    for (int z = 0; z < 7; z++) {
-                        r = fma(cxp[z], g[z] - f0, r);
-                    }
+                    for (int z = 0; z < 7; z++) r = fma(cxp[z], g[z] - f0, r);
                     gx[k] = r;
                 }
                 if (yint) {
@@ -226,12 +224,10 @@ __device__ void stage_tile(const Args &a, int st, int4 item, const T *qin, T *qo
                 } else {
                     const int o0 = (j < 3) ? -j : (in.jmax - 7 - j);
                     const T *g = q + k * plane + idx + (long long)o0 * in.pitch;
-                    const T f0 = q[k * plane + idx];
+                    const T f0 = (sizeof(T) == 4) ? q[k * plane + idx] : T(0);
                     T r = T(0);
 #pragma unroll
-                    for (int z = 0; z < 7; z++) {
-                        r = fma(cyp[z], g[(long long)z * in.pitch] - f0, r);
-                    }
+                    for (int z = 0; z < 7; z++) r = fma(cyp[z], g[(long long)z * in.pitch] - f0, r);
                     gy[k] = r;
                 }
             }
@@ -320,9 +316,22 @@ __device__ void stage_tile(const Args &a, int st, int4 item, const T *qin, T *qo
 // ---------------------------------------------------------------------------
 // Filter recurrences (constant-exact forms of ns_split.cu).
 // ---------------------------------------------------------------------------
+// Interior filter step.  FP32: the constant-exact form of ns_split.cu.
+// FP64: v = c0*u0 + sum_s m_s*(u_s + u_-s), c0 = 1 - sigmaf*df(0) (m[0]),
+// the form and operation count of the single-grid FP64 kernel.
 template <typename T>
 __device__ __forceinline__ T pass2(const T *w, const T *m)
 {
+    if constexpr (sizeof(T) == 8) {
+        T v = m[0] * w[6];
+        v = fma(m[6], w[12] + w[0], v);
+        v = fma(m[5], w[11] + w[1], v);
+        v = fma(m[4], w[10] + w[2], v);
+        v = fma(m[3], w[9] + w[3], v);
+        v = fma(m[2], w[8] + w[4], v);
+        v = fma(m[1], w[7], v);
+        return fma(m[1], w[5], v);
+    }
     const T u0 = w[6];
     T acc = m[6] * ((w[12] - u0) + (w[0] - u0));
     acc = fma(m[5], (w[11] - u0) + (w[1] - u0), acc);
@@ -333,9 +342,16 @@ __device__ __forceinline__ T pass2(const T *w, const T *m)
     return fma(m[1], w[5] - u0, u0 + acc);
 }
 
+// Boundary filter step (b[0]: FP64 holds 1 - sigmaf*dfb(0) there).
 template <typename T, int DIR>
 __device__ __forceinline__ T passb(const T *w, int p, T bm1, const T *b, T bsum)
 {
+    if constexpr (sizeof(T) == 8) {
+        T v = b[0] * w[p];
+#pragma unroll
+        for (int z = 1; z <= 5; z++) v = fma(b[z], w[p + DIR * z], v);
+        return fma(bm1, w[p - DIR], v);
+    }
     const T u0 = w[p];
     T acc = bsum * u0;
 #pragma unroll
@@ -1195,7 +1211,7 @@ int ns_batch_create(const ns_params *const *params, int n, int precision, ns_bat
             a.alpha[k] = kAlpha[k];
             a.beta[k] = kBeta[k];
         }
-        a.fm_d[0] = 0.0;
+        a.fm_d[0] = 1.0 - sigmaf * kDf[0];   // used by the FP64 form only
         for (int s = 1; s <= 6; s++) a.fm_d[s] = -sigmaf * kDf[s];
         const double *dfb[2] = {kDfbX, kDfbY};
         for (int d = 0; d < 2; d++) {
@@ -1203,14 +1219,16 @@ int ns_batch_create(const ns_params *const *params, int n, int precision, ns_bat
             double sum = 0.0;
             for (int z = 0; z < 7; z++) sum += dfb[d][z];
             a.fbsum_d[d] = -sigmaf * sum;
-            a.fb_d[d][0] = 0.0;
+            a.fb_d[d][0] = 1.0 - sigmaf * dfb[d][1];   // used by the FP64 form only
             for (int z = 1; z <= 5; z++) a.fb_d[d][z] = -sigmaf * dfb[d][z + 1];
         }
         for (int s = 0; s < 7; s++) a.fm_f[s] = (float)a.fm_d[s];
+        a.fm_f[0] = 0.f;
         for (int d = 0; d < 2; d++) {
             a.fbm1_f[d] = (float)a.fbm1_d[d];
             a.fbsum_f[d] = (float)a.fbsum_d[d];
             for (int z = 0; z < 6; z++) a.fb_f[d][z] = (float)a.fb_d[d][z];
+            a.fb_f[d][0] = 0.f;
         }
         a.bar_count = b->bar;
         a.bar_gen = b->bar + 1;
