@@ -342,6 +342,64 @@ def batch_study(args, local):
     return out
 
 
+def adjoint_study(args, local):
+    """Config-5 workload: Euler on 512x512 with M = 0.3, a Gaussian monopole
+    source field (b = 32 cells) whose amplitude is the Keys-cubic
+    interpolant of 16x16 controls ~ N(0, 1e-3) (seed 0), omega = 0.5, 2000
+    steps; loss = sum over steps of p'^2 at 32 observers on a circle of
+    radius 150 cells.  Times the plain FP64 forward (ns_step), the
+    checkpointed forward with the loss (checkpoints every 100 steps) and the
+    reverse pass (segment recompute + stage adjoints), and checks the
+    control gradient at two controls against central differences h = 1e-7."""
+    import time
+    from navierstokes_gb300 import Solver
+    from navierstokes_gb300.adjoint import Adjoint, SourceProblem
+    pb = SourceProblem(steps=args.adjoint_steps)
+    c = pb.case
+    out = {"workload": f"Euler {c.imax}x{c.jmax}, M=0.3, monopole field from 16x16 controls, "
+                       f"omega=0.5, {pb.steps} steps, 32 observers at r=150",
+           "steps": pb.steps, "checkpoint_every": args.adjoint_k}
+    with Solver(c, device=local) as s:
+        s.set_state(c.U0)
+        s.step(0, 20)
+        s.synchronize()
+        s.set_state(c.U0)
+        t0 = time.perf_counter()
+        s.step(0, pb.steps)
+        s.synchronize()
+        t_plain = time.perf_counter() - t0
+    with Adjoint(pb, checkpoint_every=args.adjoint_k, device=local) as adj:
+        adj.set_field(pb.field(pb.controls))
+        adj.forward(20)
+        adj.backward()
+        t0 = time.perf_counter()
+        loss = adj.forward()
+        t_fwd = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        gfield = adj.backward()
+        t_bwd = time.perf_counter() - t0
+        gc = pb.controls_grad(gfield)
+        fd = []
+        h = 1e-7
+        for (a, b) in [(7, 8), (8, 7)]:
+            cp = pb.controls.copy()
+            cp[a, b] += h
+            adj.set_field(pb.field(cp))
+            lp = adj.forward()
+            cp[a, b] -= 2 * h
+            adj.set_field(pb.field(cp))
+            lm = adj.forward()
+            d = (lp - lm) / (2 * h)
+            fd.append({"control": [a, b], "adjoint": gc[a, b], "fd": d,
+                       "rel_err": abs(d - gc[a, b]) / abs(gc[a, b])})
+    out.update({"loss": loss, "plain_forward_s": t_plain, "forward_with_loss_s": t_fwd,
+                "backward_s": t_bwd, "backward_over_plain_forward": t_bwd / t_plain,
+                "gradient_cost_over_plain_forward": (t_fwd + t_bwd) / t_plain,
+                "plain_forward_value": c.points * pb.steps / t_plain / 1e6, "unit": UNIT,
+                "fd_check": fd, "grad_norm": float(np.linalg.norm(gc))})
+    return out
+
+
 def cpu_baseline_sample(case, seconds=20.0):
     """Oracle on the host cores, a bounded sample of the same workload."""
     import oracle
@@ -489,6 +547,13 @@ def run_ours(args, world, rank, local, pg):
         except Exception as e:
             batched = {"failed": str(e)}
 
+    adjoint = None
+    if rank == 0 and world == 1 and not args.no_adjoint:
+        try:
+            adjoint = adjoint_study(args, local)
+        except Exception as e:
+            adjoint = {"failed": str(e)}
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
@@ -516,6 +581,8 @@ def run_ours(args, world, rank, local, pg):
             line["split_precision"] = split
         if batched is not None:
             line["batched"] = batched
+        if adjoint is not None:
+            line["adjoint"] = adjoint
         print(json.dumps(line), flush=True)
 
 
@@ -536,6 +603,10 @@ def main():
                     help="skip the batched-sweep (config-4) study")
     ap.add_argument("--batch-n", type=int, default=64)
     ap.add_argument("--batch-steps", type=int, default=300)
+    ap.add_argument("--no-adjoint", action="store_true",
+                    help="skip the discrete-adjoint (config-5) study")
+    ap.add_argument("--adjoint-steps", type=int, default=2000)
+    ap.add_argument("--adjoint-k", type=int, default=100)
     ap.add_argument("--split-error-steps", type=lambda t: [int(x) for x in t.split(",")],
                     default=[100, 500, 1000])
     args = ap.parse_args()

@@ -242,6 +242,31 @@ NS_API int ns_batch_info(ns_batch *b, int *grid, int *tile_rows, int *blocks_per
 NS_API int ns_batch_barrier_test(ns_batch *b, int extra, long long spin_limit);
 
 /*
+ * Discrete adjoint of the FP64 Euler step (inviscid = 1, nk = 4, source
+ * NS_SRC_FIELD, uniform p_b): the gradient of
+ *   L = sum over steps n = 1..N of sum over observers m of p'(x_m, y_m, t_n)^2,
+ * p' = p - p_b interpolated bilinearly, with respect to the source field
+ * S(i,j) of rk.f90:188-189 (s = sin(wf*(iter+c_k)*dt) * S).  The reverse pass
+ * transposes ccpml, both filter sweeps, bufferxy, rk_steep, the pointwise
+ * Jacobians of EULERNONLINEAR and the DRP stencils with their closures;
+ * the forward state is checkpointed every checkpoint_every steps.
+ */
+typedef struct ns_adjoint ns_adjoint;
+NS_API int ns_adjoint_create(const ns_params *p, int nobs, const double *obs_x,
+                             const double *obs_y, int checkpoint_every, ns_adjoint **out);
+NS_API void ns_adjoint_destroy(ns_adjoint *a);
+/* Replaces S (imax*jmax doubles, i fastest). */
+NS_API int ns_adjoint_set_source(ns_adjoint *a, const double *field);
+/* Forward pass from host U0 (layout NS_LAYOUT_*), nsteps steps from iter0;
+ * writes the loss. */
+NS_API int ns_adjoint_forward(ns_adjoint *a, const double *U0, int layout, int iter0,
+                              int nsteps, double *loss);
+/* Reverse pass of the last forward pass: grad_field = dL/dS (imax*jmax). */
+NS_API int ns_adjoint_backward(ns_adjoint *a, double *grad_field);
+/* The forward context (for its state and diagnostics). */
+NS_API int ns_adjoint_context(ns_adjoint *a, ns_ctx **ctx);
+
+/*
  * ns_step_noalloc -- the time step for callers that cannot allocate device
  * memory.  No counterpart in the reference: it is an addition for hosts
  * whose device memory belongs to something else (a framework or pool that

@@ -68,6 +68,13 @@ SIGNATURES = [
     ("ns_batch_info", C.c_int, [_VP, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                 C.POINTER(C.c_int), _VP]),
     ("ns_batch_barrier_test", C.c_int, [_VP, C.c_int, C.c_longlong]),
+    ("ns_adjoint_create", C.c_int, [_VP, C.c_int, _VP, _VP, C.c_int, C.POINTER(_VP)]),
+    ("ns_adjoint_destroy", None, [_VP]),
+    ("ns_adjoint_set_source", C.c_int, [_VP, _VP]),
+    ("ns_adjoint_forward", C.c_int, [_VP, _VP, C.c_int, C.c_int, C.c_int,
+                                     C.POINTER(C.c_double)]),
+    ("ns_adjoint_backward", C.c_int, [_VP, _VP]),
+    ("ns_adjoint_context", C.c_int, [_VP, C.POINTER(_VP)]),
 ]
 
 NS_KC_COUNT = 11

@@ -1,0 +1,628 @@
+// ns_adjoint.cu -- discrete adjoint of the FP64 Euler step (rk.f90:12-75,
+// 1/Re = 0, nk = 4) for the gradient of an observer loss with respect to
+// the source field.
+//
+// Forward: U_{n+1} = Phi(U_n; S), n = 0..N-1, with the source of
+// rk.f90:188-189 written as s = sin(wf*(iter+c_k)*dt) * S(i,j).  Loss
+// L = sum_n sum_m p'(x_m, t_{n+1})^2 with p' = p - p_b interpolated
+// bilinearly at observer m.  The reverse pass applies, per step and stage in
+// reverse order, the transposes of ccpml (cc.f90:6-68), lddfiltery and
+// lddfilterx (filtering.f90, in reverse sweep order), bufferxy
+// (rk.f90:77-151), rk_steep (rk.f90:153-169), EULERNONLINEAR's pointwise
+// Jacobians (eqeuler.f90:63-92) and the DRP derivatives with their closures
+// and metrics (diff.f90:6-350).  The forward state is checkpointed every K
+// steps; each K-step segment is recomputed once, keeping every stage's input
+// state and derivatives, so the reverse pass recomputes nothing.
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "ns_internal.cuh"
+
+namespace ns {
+namespace adj {
+
+// ---------------------------------------------------------------------------
+// Observers: p' at (x, y) by bilinear interpolation of the four grid points
+// around it; loss and its gradient.
+// ---------------------------------------------------------------------------
+struct Obs {
+    int i0, j0;     // lower-left grid point (0-based)
+    double wx, wy;  // fractional position in the cell
+};
+
+__device__ __forceinline__ double obs_p(const double *U, const Dims &d, const Obs &o, double pb)
+{
+    const double *p = U + 3 * d.plane;
+    const long long r0 = (long long)o.j0 * d.pitch + o.i0, r1 = r0 + d.pitch;
+    return (1 - o.wx) * (1 - o.wy) * (p[r0] - pb) + o.wx * (1 - o.wy) * (p[r0 + 1] - pb) +
+           (1 - o.wx) * o.wy * (p[r1] - pb) + o.wx * o.wy * (p[r1 + 1] - pb);
+}
+
+__global__ void k_obs_loss(const double *U, Dims d, const Obs *obs, int nobs, double pb,
+                           double *loss)
+{
+    double acc = 0.0;
+    for (int m = threadIdx.x; m < nobs; m += 32) {
+        const double v = obs_p(U, d, obs[m], pb);
+        acc += v * v;
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (threadIdx.x == 0) *loss += acc;
+}
+
+// lam_p += dL/dp of sum_m p'_m^2 at U
+__global__ void k_obs_grad(const double *U, Dims d, const Obs *obs, int nobs, double pb,
+                           double *lam)
+{
+    const int m = threadIdx.x + blockIdx.x * blockDim.x;
+    if (m >= nobs) return;
+    const Obs o = obs[m];
+    const double g = 2.0 * obs_p(U, d, o, pb);
+    double *lp = lam + 3 * d.plane;
+    const long long r0 = (long long)o.j0 * d.pitch + o.i0, r1 = r0 + d.pitch;
+    atomicAdd(lp + r0, g * (1 - o.wx) * (1 - o.wy));
+    atomicAdd(lp + r0 + 1, g * o.wx * (1 - o.wy));
+    atomicAdd(lp + r1, g * (1 - o.wx) * o.wy);
+    atomicAdd(lp + r1 + 1, g * o.wx * o.wy);
+}
+
+// ---------------------------------------------------------------------------
+// ccpml transpose.  Forward order: left, right (all rows), top, bottom (all
+// columns); transpose: bottom^T, top^T (columns), then right^T, left^T
+// (rows).  An edge value set from 2*q(1) - q(2) sends 2x and -1x of its
+// adjoint inward and is zeroed; a value set to a constant is zeroed.
+// ---------------------------------------------------------------------------
+__global__ void k_bct_cols(double *lam, Dims d)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.imax) return;
+    const long long P = d.plane, p = d.pitch;
+    const int jt = d.jmax - 1;
+    for (int k = 0; k < 4; k++) {
+        double *l = lam + k * P + i;
+        // bottom^T (cc.f90:55-59)
+        const double b = l[0];
+        if (k < 3) {
+            l[p] += 2.0 * b;
+            l[2 * p] -= b;
+        }
+        l[0] = 0.0;
+        // top^T (cc.f90:39-43)
+        const double t = l[(long long)jt * p];
+        if (k < 3) {
+            l[(long long)(jt - 1) * p] += 2.0 * t;
+            l[(long long)(jt - 2) * p] -= t;
+        }
+        l[(long long)jt * p] = 0.0;
+    }
+}
+
+__global__ void k_bct_rows(double *lam, Dims d)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= d.jmax) return;
+    const long long P = d.plane;
+    const int ir = d.imax - 1;
+    for (int k = 0; k < 4; k++) {
+        double *l = lam + k * P + (long long)j * d.pitch;
+        // right^T (cc.f90:32-36)
+        const double r = l[ir];
+        if (k < 3) {
+            l[ir - 1] += 2.0 * r;
+            l[ir - 2] -= r;
+        }
+        l[ir] = 0.0;
+        // left^T (cc.f90:23-27): only u is extrapolated
+        const double a = l[0];
+        if (k == 1) {
+            l[1] += 2.0 * a;
+            l[2] -= a;
+        }
+        l[0] = 0.0;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Filter transpose.  The forward sweep is a product of elementary updates
+// E_q (row q replaced by a combination of its neighbours); its transpose
+// applies E_q^T in reverse order: pass 3 ascending q = n-7..n-2, pass 2
+// descending q = n-7..6, pass 1 descending q = 6..1.  E_q^T adds c_s*lam_q
+// to lam_{q+s} and scales lam_q by c_0.  In the descending pass 2 a window
+// of 13 values slides down the line; after step q the value at q+6 is
+// final.  Chunks start `warm` steps above their range from the untouched
+// adjoint; the missing contributions decay as in the forward recurrence.
+// ---------------------------------------------------------------------------
+template <bool ALONG_Y>
+__global__ void __launch_bounds__(128)
+    k_filter_t(Dims d, const double *__restrict__ in, double *__restrict__ out, int chunks,
+               int warm, FilterCoef fc)
+{
+    const int nlines = ALONG_Y ? d.imax : d.jmax;
+    const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= (long long)nlines * 4 * chunks) return;
+    const int line = (int)(gid % nlines);
+    const int rest = (int)(gid / nlines);
+    const int k = rest % 4, c = rest / 4;
+    const int n = ALONG_Y ? d.jmax : d.imax;
+    const long long st = ALONG_Y ? d.pitch : 1;
+    const long long base = (long long)k * d.plane + (ALONG_Y ? line : (long long)line * d.pitch);
+    const double *__restrict__ s = in + base;
+    double *__restrict__ o = out + base;
+    const int len2 = n - 12;
+    const int a = 6 + (int)(((long long)c * len2) / chunks);
+    const int b = 6 + (int)(((long long)(c + 1) * len2) / chunks);
+    double w[13];
+    int q;
+    const int qtop = n - 7;
+    if (c == chunks - 1 || warm < 0 || b - 1 + warm >= qtop) {
+        // exact start at the top: pass 3^T on positions n-12..n-1
+        double L[12];
+#pragma unroll
+        for (int x = 0; x < 12; x++) L[x] = s[(long long)(n - 12 + x) * st];
+#pragma unroll
+        for (int x = 5; x <= 10; x++) {
+            const double lq = L[x];
+            L[x + 1] = fma(fc.bm1, lq, L[x + 1]);
+#pragma unroll
+            for (int z = 1; z <= 5; z++) L[x - z] = fma(fc.b[z], lq, L[x - z]);
+            L[x] = fc.b0 * lq;
+        }
+#pragma unroll
+        for (int x = 0; x < 12; x++) w[x + 1] = L[x];
+        w[0] = s[(long long)(n - 13) * st];
+        q = qtop;
+    } else {
+        q = b - 1 + warm;
+#pragma unroll
+        for (int t = 0; t < 13; t++) w[t] = s[(long long)(q - 6 + t) * st];
+    }
+    for (; q >= a; q--) {
+        const double lq = w[6];
+        w[0] = fma(fc.m[6], lq, w[0]);
+        w[1] = fma(fc.m[5], lq, w[1]);
+        w[2] = fma(fc.m[4], lq, w[2]);
+        w[3] = fma(fc.m[3], lq, w[3]);
+        w[4] = fma(fc.m[2], lq, w[4]);
+        w[5] = fma(fc.m[1], lq, w[5]);
+        w[7] = fma(fc.m[1], lq, w[7]);
+        w[8] = fma(fc.m[2], lq, w[8]);
+        w[9] = fma(fc.m[3], lq, w[9]);
+        w[10] = fma(fc.m[4], lq, w[10]);
+        w[11] = fma(fc.m[5], lq, w[11]);
+        w[12] = fma(fc.m[6], lq, w[12]);
+        w[6] = fc.c0 * lq;
+        if (q < b) o[(long long)(q + 6) * st] = w[12];
+#pragma unroll
+        for (int t = 12; t > 0; t--) w[t] = w[t - 1];
+        w[0] = (q - 7 >= 0) ? s[(long long)(q - 7) * st] : 0.0;
+    }
+    if (c == 0) {
+        // window now holds positions -1..11 in w[0..12]: pass 1^T, q = 6..1
+#pragma unroll
+        for (int qq = 6; qq >= 1; qq--) {
+            const double lq = w[qq + 1];
+            w[qq] = fma(fc.bm1, lq, w[qq]);
+#pragma unroll
+            for (int z = 1; z <= 5; z++) w[qq + 1 + z] = fma(fc.b[z], lq, w[qq + 1 + z]);
+            w[qq + 1] = fc.b0 * lq;
+        }
+#pragma unroll
+        for (int p = 0; p < 12; p++) o[(long long)p * st] = w[p + 1];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Pointwise part of a stage transpose: bufferxy^T, rk_steep^T and the
+// Jacobians of EULERNONLINEAR (eqeuler.f90:63-92, 1/Re = 0) at the stored
+// stage input U with its derivatives (ux = dU/dx, uy = dU/dy).
+//   in:  lam = dL/dU after the stage's buffer, om = dL/dw' (from later stages)
+//   out: lam = pointwise part of dL/dU(stage input), om = dL/dw(stage input),
+//        lx, ly = dL/d(dU/dx), dL/d(dU/dy); gS += sin_k * dL/d(dp/dt)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256)
+    k_point_t(Dims d, double *__restrict__ lam, double *__restrict__ om,
+              double *__restrict__ lx, double *__restrict__ ly, const double *__restrict__ U,
+              const double *__restrict__ ux, const double *__restrict__ uy,
+              const double *__restrict__ sigx, const double *__restrict__ sigy,
+              double *__restrict__ gS, double gamma, double dt, double alpha, double beta,
+              double sink)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= d.imax || j >= d.jmax) return;
+    const long long idx = (long long)j * d.pitch + i, P = d.plane;
+    double l[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) l[k] = lam[k * P + idx];
+    // bufferxy^T: U'' = Ub + s*(U' - Ub), y then x
+    if (i < d.D || i >= d.imax - d.D) {
+        const double s = sigx[i];
+#pragma unroll
+        for (int k = 0; k < 4; k++) l[k] *= s;
+    }
+    if (j < d.D || j >= d.jmax - d.D) {
+        const double s = sigy[j];
+#pragma unroll
+        for (int k = 0; k < 4; k++) l[k] *= s;
+    }
+    const bool interior = (i > 0) && (i < d.imax - 1) && (j > 0) && (j < d.jmax - 1);
+    double gx[4] = {0, 0, 0, 0}, gy[4] = {0, 0, 0, 0};
+    if (interior) {
+        // rk_steep^T: U1 = U + beta*w', w' = alpha*w + dt*R
+        double aR[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const double wt = fma(beta, l[k], om[k * P + idx]);
+            aR[k] = dt * wt;
+            om[k * P + idx] = alpha * wt;
+        }
+        gS[idx] = fma(sink, aR[3], gS[idx]);
+        const double rho = U[idx], uu = U[P + idx], vv = U[2 * P + idx], pp = U[3 * P + idx];
+        double dx[4], dy[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            dx[k] = ux[k * P + idx];
+            dy[k] = uy[k * P + idx];
+        }
+        const double ri = 1.0 / rho, ri2 = ri * ri;
+        const double div = dx[1] + dy[2];
+        const double a0 = aR[0], a1 = aR[1], a2 = aR[2], a3 = aR[3];
+        // f_rho = -(u rho_x + rho u_x + v rho_y + rho v_y)
+        // f_u   = -(u u_x + p_x/rho + v u_y)
+        // f_v   = -(u v_x + v v_y + p_y/rho)
+        // f_p   = -(gamma p u_x + u p_x + gamma p v_y + v p_y - s)
+        l[0] += -a0 * div + (a1 * dx[3] + a2 * dy[3]) * ri2;
+        l[1] += -(a0 * dx[0] + a1 * dx[1] + a2 * dx[2] + a3 * dx[3]);
+        l[2] += -(a0 * dy[0] + a1 * dy[1] + a2 * dy[2] + a3 * dy[3]);
+        l[3] += -a3 * gamma * div;
+        gx[0] = -uu * a0;
+        gy[0] = -vv * a0;
+        gx[1] = -rho * a0 - uu * a1 - gamma * pp * a3;
+        gy[1] = -vv * a1;
+        gx[2] = -uu * a2;
+        gy[2] = -rho * a0 - vv * a2 - gamma * pp * a3;
+        gx[3] = -ri * a1 - uu * a3;
+        gy[3] = -ri * a2 - vv * a3;
+    } else {
+#pragma unroll
+        for (int k = 0; k < 4; k++) om[k * P + idx] = 0.0;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        lam[k * P + idx] = l[k];
+        lx[k * P + idx] = gx[k];
+        ly[k * P + idx] = gy[k];
+    }
+}
+
+// Coefficient of f[q] in the derivative at row r of a line of length n
+// (the per-position tables of ns_api.cu: interior rows hold c_s in entries
+// 4..6 for sum_s c_s*(f[r+s]-f[r-s]); closure rows hold 7 coefficients for
+// offsets o0..o0+6).
+__device__ __forceinline__ double dcoef(const double *tab, int r, int q, int n)
+{
+    const double *c = tab + kCoefStride * r;
+    if (r >= 3 && r < n - 3) {
+        const int s = q - r;
+        if (s >= 1 && s <= 3) return c[3 + s];
+        if (s <= -1 && s >= -3) return -c[3 - s];
+        return 0.0;
+    }
+    const int o0 = (r < 3) ? -r : (n - 7 - r);
+    const int z = q - r - o0;
+    return (z >= 0 && z < 7) ? c[z] : 0.0;
+}
+
+// sum_r D[r][q] * g[r] along one line
+__device__ __forceinline__ double dtrans(const double *__restrict__ g, long long st, int q, int n,
+                                         const double *__restrict__ tab)
+{
+    if (q >= 9 && q < n - 9) {
+        const double *t = tab;
+        double r = 0.0;
+#pragma unroll
+        for (int s = 1; s <= 3; s++) {
+            r = fma(t[kCoefStride * (q - s) + 3 + s], g[-s * st], r);
+            r = fma(-t[kCoefStride * (q + s) + 3 + s], g[s * st], r);
+        }
+        return r;
+    }
+    double r = 0.0;
+    for (int rr = max(0, q - 6); rr <= min(n - 1, q + 6); rr++)
+        r = fma(dcoef(tab, rr, q, n), g[(long long)(rr - q) * st], r);
+    return r;
+}
+
+// lam += Dx^T lx + Dy^T ly
+__global__ void __launch_bounds__(256)
+    k_deriv_t(Dims d, double *__restrict__ lam, const double *__restrict__ lx,
+              const double *__restrict__ ly, const double *__restrict__ xcoef,
+              const double *__restrict__ ycoef)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= d.imax || j >= d.jmax) return;
+    const long long idx = (long long)j * d.pitch + i, P = d.plane;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const double v = dtrans(lx + k * P + idx, 1, i, d.imax, xcoef) +
+                         dtrans(ly + k * P + idx, d.pitch, j, d.jmax, ycoef);
+        lam[k * P + idx] += v;
+    }
+}
+
+}  // namespace adj
+}  // namespace ns
+
+// ===========================================================================
+// Host side
+// ===========================================================================
+struct ns_adjoint {
+    ns_ctx *fwd = nullptr;
+    int nobs = 0, K = 100, nsteps = 0, iter0 = 0;
+    double pb = 0.0;
+    ns::adj::Obs *obs = nullptr;
+    double *loss = nullptr;
+    double *chk = nullptr;     // checkpoints: nchk x 4 planes
+    int nchk = 0;
+    double *store = nullptr;   // segment: K steps x 6 stages x 12 planes (U, dU/dx, dU/dy)
+    double *endstate = nullptr;
+    double *lam = nullptr, *lam2 = nullptr, *om = nullptr, *lx = nullptr, *ly = nullptr;
+    double *gS = nullptr;
+    double *dudm0 = nullptr, *dudn0 = nullptr;  // the context's own derivative planes
+    double sin_host[6];
+    bool forward_done = false;
+    std::string err;
+};
+
+namespace {
+
+int aerr(ns_adjoint *a, int code, const std::string &m)
+{
+    if (a) a->err = m;
+    ns::record_error(m.c_str());
+    return code;
+}
+
+#define A_CUDA(a, call)                                                                      \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess) return aerr((a), NS_ERR_CUDA, std::string(#call ": ") + cudaGetErrorString(e_)); \
+    } while (0)
+
+// sin(wf*((iter+c_k)*dt)) of rk.f90:188 for the six stages of step `iter`
+void stage_sines(const ns_ctx *c, int iter, double *out)
+{
+    for (int k = 0; k < 6; k++) out[k] = std::sin(c->p.wf * (((double)iter + c->ct[k]) * c->p.dt));
+}
+
+// One forward step stage by stage; when `slot` is non-null, each stage's
+// input U and its derivatives are kept there (12 planes per stage).
+int forward_step(ns_adjoint *a, int iter, double *slot)
+{
+    ns_ctx *c = a->fwd;
+    const size_t P = (size_t)c->d.plane;
+    cudaStream_t s = c->stream;
+    int cls[ns::kMaxStepLaunches], stg[ns::kMaxStepLaunches];
+    const int n = ns::step_sequence(c, cls, stg);
+    A_CUDA(a, ns::launch_set_iter(c->d_iter, iter, s));
+    for (int q = 0; q < n; q++) {
+        if (slot && cls[q] == NS_KC_FIRST) {
+            double *base = slot + (size_t)stg[q] * 12 * P;
+            A_CUDA(a, cudaMemcpyAsync(base, c->U, 4 * P * sizeof(double), cudaMemcpyDeviceToDevice, s));
+            c->dudm = base + 4 * P;
+            c->dudn = base + 8 * P;
+        }
+        A_CUDA(a, ns::launch_kernel(c, cls[q], stg[q], s));
+        if (slot && cls[q] == NS_KC_UPDATE) {
+            c->dudm = a->dudm0;
+            c->dudn = a->dudn0;
+        }
+    }
+    return NS_OK;
+}
+
+int stage_adjoint(ns_adjoint *a, const double *slot, int stage, double sink)
+{
+    ns_ctx *c = a->fwd;
+    const ns::Dims &d = c->d;
+    const size_t P = (size_t)d.plane;
+    cudaStream_t s = c->stream;
+    const double *U = slot + (size_t)stage * 12 * P;
+    ns::adj::k_bct_cols<<<(d.imax + 127) / 128, 128, 0, s>>>(a->lam, d);
+    ns::adj::k_bct_rows<<<(d.jmax + 127) / 128, 128, 0, s>>>(a->lam, d);
+    {
+        const long long ty = (long long)d.imax * 4 * c->fy_chunks;
+        ns::adj::k_filter_t<true><<<(unsigned)((ty + 127) / 128), 128, 0, s>>>(
+            d, a->lam, a->lam2, c->fy_chunks, c->warm, c->fy);
+        const long long tx = (long long)d.jmax * 4 * c->fx_chunks;
+        ns::adj::k_filter_t<false><<<(unsigned)((tx + 127) / 128), 128, 0, s>>>(
+            d, a->lam2, a->lam, c->fx_chunks, c->warm, c->fx);
+    }
+    const dim3 blk(32, 8), grd((d.imax + 31) / 32, (d.jmax + 7) / 8);
+    ns::adj::k_point_t<<<grd, blk, 0, s>>>(d, a->lam, a->om, a->lx, a->ly, U, U + 4 * P, U + 8 * P,
+                                           c->sigx, c->sigy, a->gS, c->phys.gamma, c->p.dt,
+                                           c->alpha[stage], c->beta[stage], sink);
+    ns::adj::k_deriv_t<<<grd, blk, 0, s>>>(d, a->lam, a->lx, a->ly, c->xcoef, c->ycoef);
+    A_CUDA(a, cudaGetLastError());
+    return NS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ns_adjoint_create(const ns_params *p, int nobs, const double *obs_x, const double *obs_y,
+                      int checkpoint_every, ns_adjoint **out)
+{
+    if (!out || !p || nobs < 1 || !obs_x || !obs_y || checkpoint_every < 1)
+        return aerr(nullptr, NS_ERR_PARAM, "ns_adjoint_create: bad argument");
+    *out = nullptr;
+    if (!p->inviscid || p->nk != 4 || p->precision != NS_PREC_FP64 ||
+        p->source_mode != NS_SRC_FIELD || !p->m || !p->n)
+        return aerr(nullptr, NS_ERR_UNSUPPORTED,
+                    "ns_adjoint_create: the adjoint covers the FP64 Euler step (inviscid=1, nk=4) "
+                    "with a source field (NS_SRC_FIELD) and coordinates m, n");
+    ns_adjoint *a = new (std::nothrow) ns_adjoint();
+    if (!a) return aerr(nullptr, NS_ERR_OOM, "ns_adjoint_create: host allocation");
+    int rc = ns_create(p, &a->fwd);
+    if (rc != NS_OK) {
+        delete a;
+        return rc;
+    }
+    ns_ctx *c = a->fwd;
+    a->K = checkpoint_every;
+    a->nobs = nobs;
+    a->dudm0 = c->dudm;
+    a->dudn0 = c->dudn;
+    // base pressure (uniform p_b is required: the loss is on p - p_b)
+    a->pb = p->ub_layout == NS_LAYOUT_FORTRAN ? p->Ub[3] : p->Ub[3 * (size_t)p->imax * p->jmax];
+    std::vector<ns::adj::Obs> ob(nobs);
+    const double x0 = p->m[0], y0 = p->n[0];
+    for (int q = 0; q < nobs; q++) {
+        const double fx = (obs_x[q] - x0) / p->dm, fy = (obs_y[q] - y0) / p->dn;
+        const int i0 = (int)std::floor(fx), j0 = (int)std::floor(fy);
+        if (i0 < 0 || j0 < 0 || i0 + 1 >= p->imax || j0 + 1 >= p->jmax) {
+            ns_destroy(c);
+            delete a;
+            return aerr(nullptr, NS_ERR_PARAM, "ns_adjoint_create: observer outside the grid");
+        }
+        ob[q] = {i0, j0, fx - i0, fy - j0};
+    }
+    const size_t P = (size_t)c->d.plane;
+    cudaError_t e = cudaMalloc(&a->obs, nobs * sizeof(ns::adj::Obs));
+    if (e == cudaSuccess) e = cudaMalloc(&a->loss, sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&a->store, (size_t)a->K * 6 * 12 * P * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&a->endstate, 4 * P * sizeof(double));
+    double **bufs[] = {&a->lam, &a->lam2, &a->om, &a->lx, &a->ly};
+    for (double **b : bufs)
+        if (e == cudaSuccess) e = cudaMalloc(b, 4 * P * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&a->gS, P * sizeof(double));
+    if (e == cudaSuccess)
+        e = cudaMemcpy(a->obs, ob.data(), nobs * sizeof(ns::adj::Obs), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        rc = aerr(nullptr, NS_ERR_OOM, std::string("ns_adjoint_create: ") + cudaGetErrorString(e));
+        ns_adjoint_destroy(a);
+        return rc;
+    }
+    *out = a;
+    return NS_OK;
+}
+
+void ns_adjoint_destroy(ns_adjoint *a)
+{
+    if (!a) return;
+    if (a->fwd) {
+        cudaSetDevice(a->fwd->dev);
+        cudaStreamSynchronize(a->fwd->stream);
+        a->fwd->dudm = a->dudm0;
+        a->fwd->dudn = a->dudn0;
+    }
+    void *ps[] = {a->obs, a->loss, a->chk, a->store, a->endstate, a->lam, a->lam2, a->om,
+                  a->lx, a->ly, a->gS};
+    for (void *p : ps)
+        if (p) cudaFree(p);
+    if (a->fwd) ns_destroy(a->fwd);
+    delete a;
+}
+
+// Replaces the source field S (imax*jmax doubles, i fastest).
+int ns_adjoint_set_source(ns_adjoint *a, const double *field)
+{
+    if (!a || !field) return aerr(a, NS_ERR_PARAM, "ns_adjoint_set_source: NULL argument");
+    ns_ctx *c = a->fwd;
+    const size_t row = (size_t)c->d.imax * sizeof(double);
+    A_CUDA(a, cudaMemcpy2DAsync(c->src, c->d.pitch * sizeof(double), field, row, row,
+                                (size_t)c->d.jmax, cudaMemcpyHostToDevice, c->stream));
+    A_CUDA(a, cudaStreamSynchronize(c->stream));
+    a->forward_done = false;
+    return NS_OK;
+}
+
+// Forward pass from U0 (host, layout as ns_set_state) for nsteps steps with
+// iter = iter0.. ; checkpoints every K steps; *loss = the observer loss.
+int ns_adjoint_forward(ns_adjoint *a, const double *U0, int layout, int iter0, int nsteps,
+                       double *loss)
+{
+    if (!a || !U0 || nsteps < 1 || !loss) return aerr(a, NS_ERR_PARAM, "ns_adjoint_forward: bad argument");
+    ns_ctx *c = a->fwd;
+    const size_t P = (size_t)c->d.plane;
+    int rc = ns_set_state(c, U0, layout);
+    if (rc != NS_OK) return rc;
+    const int nchk = (nsteps + a->K - 1) / a->K;
+    if (nchk > a->nchk) {
+        if (a->chk) cudaFree(a->chk);
+        a->chk = nullptr;
+        A_CUDA(a, cudaMalloc(&a->chk, (size_t)nchk * 4 * P * sizeof(double)));
+        a->nchk = nchk;
+    }
+    cudaStream_t s = c->stream;
+    A_CUDA(a, cudaMemsetAsync(a->loss, 0, sizeof(double), s));
+    for (int n = 0; n < nsteps; n++) {
+        if (n % a->K == 0)
+            A_CUDA(a, cudaMemcpyAsync(a->chk + (size_t)(n / a->K) * 4 * P, c->U, 4 * P * sizeof(double),
+                                      cudaMemcpyDeviceToDevice, s));
+        rc = ns_step(c, iter0 + n, 1);
+        if (rc != NS_OK) return rc;
+        ns::adj::k_obs_loss<<<1, 32, 0, s>>>(c->U, c->d, a->obs, a->nobs, a->pb, a->loss);
+    }
+    A_CUDA(a, cudaMemcpyAsync(a->endstate, c->U, 4 * P * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    A_CUDA(a, cudaMemcpyAsync(loss, a->loss, sizeof(double), cudaMemcpyDeviceToHost, s));
+    A_CUDA(a, cudaStreamSynchronize(s));
+    a->nsteps = nsteps;
+    a->iter0 = iter0;
+    a->forward_done = true;
+    return NS_OK;
+}
+
+// Reverse pass: grad_field[imax*jmax] (i fastest) = dL/dS.
+int ns_adjoint_backward(ns_adjoint *a, double *grad_field)
+{
+    if (!a || !grad_field) return aerr(a, NS_ERR_PARAM, "ns_adjoint_backward: NULL argument");
+    if (!a->forward_done) return aerr(a, NS_ERR_STATE, "ns_adjoint_backward before ns_adjoint_forward");
+    ns_ctx *c = a->fwd;
+    const ns::Dims &d = c->d;
+    const size_t P = (size_t)d.plane;
+    cudaStream_t s = c->stream;
+    A_CUDA(a, cudaMemsetAsync(a->lam, 0, 4 * P * sizeof(double), s));
+    A_CUDA(a, cudaMemsetAsync(a->gS, 0, P * sizeof(double), s));
+    const int nseg = (a->nsteps + a->K - 1) / a->K;
+    int rc;
+    for (int sg = nseg - 1; sg >= 0; sg--) {
+        const int n0 = sg * a->K, n1 = std::min(a->nsteps, n0 + a->K);
+        // recompute the segment, keeping every stage's input and derivatives
+        A_CUDA(a, cudaMemcpyAsync(c->U, a->chk + (size_t)sg * 4 * P, 4 * P * sizeof(double),
+                                  cudaMemcpyDeviceToDevice, s));
+        for (int n = n0; n < n1; n++)
+            if ((rc = forward_step(a, a->iter0 + n, a->store + (size_t)(n - n0) * 6 * 12 * P)) != NS_OK)
+                return rc;
+        for (int n = n1 - 1; n >= n0; n--) {
+            // loss term of U_{n+1}: the state after step n
+            const double *Unext = (n == n1 - 1) ? c->U : a->store + (size_t)(n + 1 - n0) * 6 * 12 * P;
+            ns::adj::k_obs_grad<<<(a->nobs + 63) / 64, 64, 0, s>>>(Unext, d, a->obs, a->nobs, a->pb, a->lam);
+            A_CUDA(a, cudaMemsetAsync(a->om, 0, 4 * P * sizeof(double), s));
+            double sn[6];
+            stage_sines(c, a->iter0 + n, sn);
+            const double *slot = a->store + (size_t)(n - n0) * 6 * 12 * P;
+            for (int st = 5; st >= 0; st--)
+                if ((rc = stage_adjoint(a, slot, st, sn[st])) != NS_OK) return rc;
+        }
+    }
+    const size_t row = (size_t)d.imax * sizeof(double);
+    A_CUDA(a, cudaMemcpy2DAsync(grad_field, row, a->gS, d.pitch * sizeof(double), row,
+                                (size_t)d.jmax, cudaMemcpyDeviceToHost, s));
+    A_CUDA(a, cudaStreamSynchronize(s));
+    // leave the context's state at the forward end state
+    A_CUDA(a, cudaMemcpy(c->U, a->endstate, 4 * P * sizeof(double), cudaMemcpyDeviceToDevice));
+    return NS_OK;
+}
+
+int ns_adjoint_context(ns_adjoint *a, ns_ctx **ctx)
+{
+    if (!a || !ctx) return aerr(a, NS_ERR_PARAM, "ns_adjoint_context: NULL argument");
+    *ctx = a->fwd;
+    return NS_OK;
+}
+
+}  // extern "C"
