@@ -133,6 +133,33 @@ __global__ void k_bct_rows(double *lam, Dims d)
 // final.  Chunks start `warm` steps above their range from the untouched
 // adjoint; the missing contributions decay as in the forward recurrence.
 // ---------------------------------------------------------------------------
+// E_q^T of one pass-2 point q = w[6]: w[0..12] hold the adjoint at q-6..q+6.
+__device__ __forceinline__ void transpose13(const FilterCoef &fc, double *w)
+{
+    const double lq = w[6];
+    w[0] = fma(fc.m[6], lq, w[0]);
+    w[1] = fma(fc.m[5], lq, w[1]);
+    w[2] = fma(fc.m[4], lq, w[2]);
+    w[3] = fma(fc.m[3], lq, w[3]);
+    w[4] = fma(fc.m[2], lq, w[4]);
+    w[5] = fma(fc.m[1], lq, w[5]);
+    w[7] = fma(fc.m[1], lq, w[7]);
+    w[8] = fma(fc.m[2], lq, w[8]);
+    w[9] = fma(fc.m[3], lq, w[9]);
+    w[10] = fma(fc.m[4], lq, w[10]);
+    w[11] = fma(fc.m[5], lq, w[11]);
+    w[12] = fma(fc.m[6], lq, w[12]);
+    w[6] = fc.c0 * lq;
+}
+
+// Slides the window one point down; `next` is the untouched adjoint at q-7.
+__device__ __forceinline__ void shift13_down(double *w, double next)
+{
+#pragma unroll
+    for (int t = 12; t > 0; t--) w[t] = w[t - 1];
+    w[0] = next;
+}
+
 template <bool ALONG_Y>
 __global__ void __launch_bounds__(128)
     k_filter_t(Dims d, const double *__restrict__ in, double *__restrict__ out, int chunks,
@@ -177,25 +204,32 @@ __global__ void __launch_bounds__(128)
 #pragma unroll
         for (int t = 0; t < 13; t++) w[t] = s[(long long)(q - 6 + t) * st];
     }
-    for (; q >= a; q--) {
-        const double lq = w[6];
-        w[0] = fma(fc.m[6], lq, w[0]);
-        w[1] = fma(fc.m[5], lq, w[1]);
-        w[2] = fma(fc.m[4], lq, w[2]);
-        w[3] = fma(fc.m[3], lq, w[3]);
-        w[4] = fma(fc.m[2], lq, w[4]);
-        w[5] = fma(fc.m[1], lq, w[5]);
-        w[7] = fma(fc.m[1], lq, w[7]);
-        w[8] = fma(fc.m[2], lq, w[8]);
-        w[9] = fma(fc.m[3], lq, w[9]);
-        w[10] = fma(fc.m[4], lq, w[10]);
-        w[11] = fma(fc.m[5], lq, w[11]);
-        w[12] = fma(fc.m[6], lq, w[12]);
-        w[6] = fc.c0 * lq;
-        if (q < b) o[(long long)(q + 6) * st] = w[12];
+    // blocks of kFilterPf points, the next block's input loaded ahead
+    double nx[kFilterPf];
 #pragma unroll
-        for (int t = 12; t > 0; t--) w[t] = w[t - 1];
-        w[0] = (q - 7 >= 0) ? s[(long long)(q - 7) * st] : 0.0;
+    for (int t = 0; t < kFilterPf; t++) {
+        const int r = q - 7 - t;
+        nx[t] = (r >= 0) ? s[(long long)r * st] : 0.0;
+    }
+    for (; q - kFilterPf + 1 >= a; q -= kFilterPf) {
+        double cur[kFilterPf];
+#pragma unroll
+        for (int t = 0; t < kFilterPf; t++) {
+            cur[t] = nx[t];
+            const int r = q - kFilterPf - 7 - t;
+            nx[t] = (r >= 0) ? s[(long long)r * st] : 0.0;
+        }
+#pragma unroll
+        for (int t = 0; t < kFilterPf; t++) {
+            transpose13(fc, w);
+            if (q - t < b) o[(long long)(q - t + 6) * st] = w[12];
+            shift13_down(w, cur[t]);
+        }
+    }
+    for (; q >= a; q--) {
+        transpose13(fc, w);
+        if (q < b) o[(long long)(q + 6) * st] = w[12];
+        shift13_down(w, (q - 7 >= 0) ? s[(long long)(q - 7) * st] : 0.0);
     }
     if (c == 0) {
         // window now holds positions -1..11 in w[0..12]: pass 1^T, q = 6..1

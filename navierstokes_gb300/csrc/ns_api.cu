@@ -210,10 +210,40 @@ int choose_chunks(int nlines_total, int n, int warm, int target_threads)
     if (warm < 0) return 1;
     const int len2 = n - 12;
     int c = (target_threads + nlines_total - 1) / nlines_total;
-    const int maxc = len2 / (4 * (warm + 6));
+    // chunks at least 4x the warm-up long (<= 25% extra work) while that
+    // still fills the GPU; when it does not (few, short lines: the filters are
+    // then latency-bound), chunks down to the warm-up length
+    int maxc = len2 / (4 * (warm + 6));
+    if ((long long)maxc * nlines_total < target_threads) maxc = len2 / (warm + 6);
     if (c > maxc) c = maxc;
     if (c < 1) c = 1;
     return c;
+}
+
+// Chunks per line of the FP64 filters.  They are bound by the FP64 pipe of
+// each SM sub-partition, which one resident warp keeps busy (a DFMA warp
+// instruction occupies it for ~67 cycles, longer than the prefetched loads'
+// latency), so the time of a launch is about (warps on the busiest
+// sub-partition) x (points per thread).  Blocks of 128 threads put one warp
+// on each sub-partition of an SM; a chunk after the first also filters
+// `warm` points of warm-up.  Picks the count with the least such time.
+int choose_chunks_fp64(int nlines_total, int n, int warm, int nsm)
+{
+    if (warm < 0) return 1;
+    const int len2 = n - 12;
+    const int maxc = std::max(1, len2 / (warm + 6));
+    int best = 1;
+    long long best_cost = -1;
+    for (int c = 1; c <= maxc; c++) {
+        const long long blocks = ((long long)nlines_total * c + 127) / 128;
+        const long long per_smsp = (blocks + nsm - 1) / nsm;
+        const long long cost = per_smsp * ((len2 + c - 1) / c + (c > 1 ? warm : 0));
+        if (best_cost < 0 || cost < best_cost) {
+            best_cost = cost;
+            best = c;
+        }
+    }
+    return best;
 }
 
 template <class T>
@@ -640,9 +670,8 @@ constants:
         c->warm = filter_warmup(p->sigmaf);
         int nsm = 152;
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->dev);
-        const int target = nsm * 4 * 2 * 32;  // about two warps per SM sub-partition
-        c->fx_chunks = choose_chunks(d.jmax * d.nk, d.imax, c->warm, target);
-        c->fy_chunks = choose_chunks(d.imax * d.nk, d.jmax, c->warm, target);
+        c->fx_chunks = choose_chunks_fp64(d.jmax * d.nk, d.imax, c->warm, nsm);
+        c->fy_chunks = choose_chunks_fp64(d.imax * d.nk, d.jmax, c->warm, nsm);
         if (c->split) {
             // FP32 filters are bound by memory: aim at 32 resident warps per SM
             ns::SplitState &sp = c->sp;

@@ -41,6 +41,9 @@ struct Dims {
 // at each end, entries 0..6 hold the 7 one-sided coefficients for offsets
 // o0..o0+6 (o0 = -q at the left end, n-7-q at the right end).
 constexpr int kCoefStride = 8;
+// Points per block of the FP64 filter recurrences (loads issued one block
+// ahead).
+constexpr int kFilterPf = 8;
 
 // Filter coefficients pre-multiplied by the filter strength.
 struct FilterCoef {

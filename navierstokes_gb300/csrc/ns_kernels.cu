@@ -261,6 +261,33 @@ __global__ void __launch_bounds__(256)
 // recurrence at every point, and `warm` is chosen on the host so that it
 // falls below 2^-60 of the data before the chunk's first output.
 // ---------------------------------------------------------------------------
+// One pass-2 point: w[0..5] filtered points q-6..q-1, w[6..12] unfiltered
+// points q..q+6.
+__device__ __forceinline__ double filter13(const FilterCoef &fc, const double *w)
+{
+    double v = fc.c0 * w[6];
+    v = fma(fc.m[6], w[12] + w[0], v);
+    v = fma(fc.m[5], w[11] + w[1], v);
+    v = fma(fc.m[4], w[10] + w[2], v);
+    v = fma(fc.m[3], w[9] + w[3], v);
+    v = fma(fc.m[2], w[8] + w[4], v);
+    v = fma(fc.m[1], w[7], v);
+    v = fma(fc.m[1], w[5], v);
+    return v;
+}
+
+// Slides the window one point: v becomes filtered point q, `next` is
+// unfiltered point q+7.
+__device__ __forceinline__ void shift13(double *w, double v, double next)
+{
+#pragma unroll
+    for (int t = 0; t < 5; t++) w[t] = w[t + 1];
+    w[5] = v;
+#pragma unroll
+    for (int t = 6; t < 12; t++) w[t] = w[t + 1];
+    w[12] = next;
+}
+
 template <bool ALONG_Y>
 __global__ void __launch_bounds__(128)
     k_filter(Dims d, const double *__restrict__ src, double *__restrict__ dst, int chunks,
@@ -309,23 +336,34 @@ __global__ void __launch_bounds__(128)
 #pragma unroll
         for (int t = 0; t < 13; t++) w[t] = s[(long long)(q - 6 + t) * st];
     }
-    // pass 2 (filtering.f90:69-79 / :161-171)
+    // pass 2 (filtering.f90:69-79 / :161-171).  Blocks of kFilterPf points,
+    // the next block's input loaded before the current block is filtered, so
+    // that a thread keeps kFilterPf loads in flight when few lines run.
+    double nx[kFilterPf];
+#pragma unroll
+    for (int t = 0; t < kFilterPf; t++) {
+        const int r = q + 7 + t;
+        nx[t] = (r < n) ? s[(long long)r * st] : 0.0;
+    }
+    for (; q + kFilterPf <= b; q += kFilterPf) {
+        double cur[kFilterPf];
+#pragma unroll
+        for (int t = 0; t < kFilterPf; t++) {
+            cur[t] = nx[t];
+            const int r = q + kFilterPf + 7 + t;
+            nx[t] = (r < n) ? s[(long long)r * st] : 0.0;
+        }
+#pragma unroll
+        for (int t = 0; t < kFilterPf; t++) {
+            const double v = filter13(fc, w);
+            if (q + t >= a) o[(long long)(q + t) * st] = v;
+            shift13(w, v, cur[t]);
+        }
+    }
     for (; q < b; q++) {
-        double v = fc.c0 * w[6];
-        v = fma(fc.m[6], w[12] + w[0], v);
-        v = fma(fc.m[5], w[11] + w[1], v);
-        v = fma(fc.m[4], w[10] + w[2], v);
-        v = fma(fc.m[3], w[9] + w[3], v);
-        v = fma(fc.m[2], w[8] + w[4], v);
-        v = fma(fc.m[1], w[7], v);
-        v = fma(fc.m[1], w[5], v);
+        const double v = filter13(fc, w);
         if (q >= a) o[(long long)q * st] = v;
-#pragma unroll
-        for (int t = 0; t < 5; t++) w[t] = w[t + 1];
-        w[5] = v;
-#pragma unroll
-        for (int t = 6; t < 12; t++) w[t] = w[t + 1];
-        w[12] = (q + 7 < n) ? s[(long long)(q + 7) * st] : 0.0;
+        shift13(w, v, (q + 7 < n) ? s[(long long)(q + 7) * st] : 0.0);
     }
     if (last) {
         // pass 3 (filtering.f90:84-94 / :176-188): w[0..11] = positions n-12..n-1
