@@ -50,7 +50,11 @@ typedef enum ns_status {
 enum {
     NS_LAYOUT_FORTRAN = 0, /* U(nk,imax,jmax), column-major: the reference's
                               own array (euler.f90:107) */
-    NS_LAYOUT_SOA = 1      /* U[k][j][i], i fastest: one plane per variable */
+    NS_LAYOUT_SOA = 1,     /* U[k][j][i], i fastest: one plane per variable */
+    NS_LAYOUT_ROWS = 2     /* a field constant along i, given by rows:
+                              nk*jmax values, k fastest, (k,j) -> U(k,:,j);
+                              expanded on the device (Ub of init.f90:387-396
+                              and the initial U = Ub of :376-384) */
 };
 
 /* Arithmetic of the stage loop. */
@@ -265,6 +269,102 @@ NS_API int ns_adjoint_forward(ns_adjoint *a, const double *U0, int layout, int i
 NS_API int ns_adjoint_backward(ns_adjoint *a, double *grad_field);
 /* The forward context (for its state and diagnostics). */
 NS_API int ns_adjoint_context(ns_adjoint *a, ns_ctx **ctx);
+
+/*
+ * The program around the step: euler.f90's time loop with its probes and
+ * field dumps, the dados.in reader and the grid/base-flow setup of init.f90.
+ * None of these is on the reference's rk.f90 boundary; they replace
+ * euler.f90:36-206, init.f90:10-52 (init_read), :56-210 (init_dados) and
+ * :341-404 (init_variables), and outt.f90:17-55 (output).
+ */
+
+/* The dados.in namelists (dados.in:1-85) as init_read reads them
+ * (init.f90:18-23): &grid (imax..ctd), &freq, &freeadm, &flow, a second
+ * &grid (D, c1b, c2b, c3b: the namelist statement at init.f90:22 extends
+ * group grid), &mpi.  Names the file does not set stay 0. */
+typedef struct ns_dados {
+    int32_t imax, jmax, maxit, cgd, cfd, ctd;  /* &grid */
+    int32_t D;                                 /* &grid (second group) */
+    int32_t iterw;                             /* &freq */
+    int32_t num_procs_x, num_procs_y;          /* &mpi */
+    double dt, sigmaf;                         /* &grid */
+    double r0_acous, amplitude, m_pt_acous, n_pt_acous, wfi, wff, wf;  /* &freq */
+    double pxfft[5];                           /* &freq pxfft1..pxfft5 */
+    double mmin, mmax, nmin, nmax;             /* &freeadm */
+    double pxr[3], pyr[3];                     /* &freeadm pxr1..3, pyr1..3 */
+    double U1, U2, Re, Pr, T1, T2, Tref;       /* &flow */
+    double c1b, c2b, c3b;                      /* &grid (second group) */
+} ns_dados;
+
+/* init_read (init.f90:10-52): reads the six groups in order, each found by
+ * scanning forward from the end of the previous one.  Accepts '!' comments,
+ * ',' or blanks between items, REAL(8) constants with d/D/e/E exponents and
+ * the terminators '/', '&end' and '$end' (dados.in:85).  A name outside the
+ * group, a malformed value, a missing group or a missing terminator is
+ * NS_ERR_PARAM with the line in ns_last_error(NULL).  ns_parse_dados takes
+ * the file's text. */
+NS_API int ns_read_dados(const char *path, ns_dados *out);
+NS_API int ns_parse_dados(const char *text, ns_dados *out);
+
+/* init_dados (init.f90:56-210): coordinates m[imax], n[jmax], buffer
+ * metrics meshx, meshy, damping sigmax, sigmay (quirk_buffer = 1: the left
+ * and bottom sigma stay 0 as in the reference, whose imaxpml/jmaxpml are
+ * never set), dm_dn[2] = {dm, dn} and the 1-based probe points
+ * probe_ij[6] = {px1, py1, px2, py2, px3, py3} (init.f90:80-85). */
+NS_API int ns_dados_grid(const ns_dados *d, int quirk_buffer, double *m, double *n,
+                         double *meshx, double *meshy, double *sigmax, double *sigmay,
+                         double *dm_dn, int32_t *probe_ij);
+
+/* Base-flow rows of init_variables (init.f90:359-373): the tanh mixing
+ * layer uba, Tb, rhob = 1/Tb and psib on the rows n[jmax]. */
+NS_API int ns_dados_profiles(const ns_dados *d, const double *n, double *uba, double *Tb,
+                             double *rhob, double *psib);
+
+/* A context for the dados.in case: Navier-Stokes with Re, Pr, Tref, nk = 4
+ * or 5 variables, the Gaussian source of rk.f90:171-193, band metrics; Ub
+ * is built on the device from its rows and the state starts at U = Ub
+ * (init.f90:376-404), so no full-size host array is made. */
+NS_API int ns_create_dados(const ns_dados *d, int nk, int device, int quirk_buffer,
+                           ns_ctx **out);
+
+/* Vorticity of the output path (outt.f90:43-49): diffall.f90's DRP
+ * derivatives, which apply no metric, on the device: omega = dv/dx - du/dy
+ * at every point, copied to omega[imax*jmax] (host, i fastest). */
+NS_API int ns_vorticity(ns_ctx *ctx, double *omega);
+
+/* One contorno_<icount>.dat file (outt.f90:40-55): per point the
+ * list-directed record m(i), n(j), rho, u, v, p, omega, psi (psi only when
+ * nk = 5), j fastest, an empty record after each i.  m, n: host coordinate
+ * arrays [imax], [jmax]. */
+NS_API int ns_write_contorno(ns_ctx *ctx, const char *path, const double *m, const double *n);
+
+/* One REAL(8) item as list-directed output writes it (G25.17 with a three-
+ * digit exponent: F20.(16-e) and five blanks for 0.1 <= |x| < 1e17, else
+ * E25.17E3 with one digit before the point); buf gets the 25 characters
+ * and a NUL.  Returns the field width, or -1 if len < 26. */
+NS_API int ns_format_real(double x, char *buf, int len);
+
+/* Probe recorder for the time loop: ns_probes_arm sets npts points
+ * (1-based pi, pj) and room for `capacity` records; each ns_probes_capture
+ * enqueues a copy of U(1..nk) at every point as the next record (no host
+ * synchronisation); ns_probes_drain copies the records taken so far,
+ * out[rec][point][k], sets *nrec and empties the recorder.  Capturing into
+ * a full recorder is NS_ERR_STATE. */
+NS_API int ns_probes_arm(ns_ctx *ctx, int npts, const int32_t *pi, const int32_t *pj,
+                         int capacity);
+NS_API int ns_probes_capture(ns_ctx *ctx);
+NS_API int ns_probes_drain(ns_ctx *ctx, double *out, int *nrec);
+
+/* The euler.f90 program (euler.f90:36-206) on the GPU: reads dados_path,
+ * sets up the case (init.f90), runs iter = 0..maxit (maxit < 0: the
+ * file's), and writes, in outdir, temp1_D60.dat .. temp3_D60.dat (t and
+ * U(1..4) at the three probe points every ctd steps) and contorno_<n>.dat
+ * every cgd steps, with the reference's screen lines on stdout.
+ * flags: NS_RUN_NO_CONTORNO skips the field files, NS_RUN_QUIET the screen
+ * lines. */
+enum { NS_RUN_NO_CONTORNO = 1, NS_RUN_QUIET = 2 };
+NS_API int ns_run_euler(const char *dados_path, const char *outdir, int nk, int device,
+                        int maxit, int flags);
 
 /*
  * ns_step_noalloc -- the time step for callers that cannot allocate device

@@ -17,6 +17,7 @@ PKG = Path(__file__).resolve().parent
 ROOT = PKG.parent
 CSRC = PKG / "csrc"
 LIB = PKG / "libns_gb300.so"
+DRIVER = PKG / "ns_euler"
 BUILD_DIR = PKG / "_build"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
@@ -31,7 +32,7 @@ def _nvcc() -> str:
 
 
 def sources() -> list[Path]:
-    return sorted(CSRC.glob("*.cu"))
+    return sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cpp"))
 
 
 def _stale(target: Path, deps: list[Path]) -> bool:
@@ -44,7 +45,10 @@ def _stale(target: Path, deps: list[Path]) -> bool:
 def build(verbose: bool = False, force: bool = False) -> Path:
     srcs = sources()
     headers = list(CSRC.glob("*.cuh")) + list((ROOT / "include").glob("*.h"))
+    drv = [CSRC / "main" / "ns_euler.cpp"]
     if not force and not _stale(LIB, srcs + headers + [Path(__file__)]):
+        if _stale(DRIVER, drv + [LIB]):
+            _build_driver()
         return LIB
     nvcc = _nvcc()
     BUILD_DIR.mkdir(exist_ok=True)
@@ -67,7 +71,23 @@ def build(verbose: bool = False, force: bool = False) -> Path:
     if r.returncode != 0:
         raise RuntimeError(f"link of libns_gb300.so failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    _build_driver()
     return LIB
+
+
+def _build_driver() -> None:
+    """ns_euler, the euler.f90 program over the library (rpath $ORIGIN)."""
+    src = CSRC / "main" / "ns_euler.cpp"
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if not cxx:
+        raise RuntimeError("a C++ compiler is required to build ns_euler")
+    tmp = DRIVER.with_suffix(".tmp")
+    cmd = [cxx, "-O2", "-std=c++17", "-I", str(ROOT / "include"), str(src), "-o", str(tmp),
+           "-L", str(PKG), "-lns_gb300", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"build of ns_euler failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, DRIVER)
 
 
 if __name__ == "__main__":

@@ -21,6 +21,7 @@ NS_ERR_UNSUPPORTED = 7
 
 NS_LAYOUT_FORTRAN = 0
 NS_LAYOUT_SOA = 1
+NS_LAYOUT_ROWS = 2
 NS_PREC_FP64 = 0
 NS_PREC_SPLIT = 1
 NS_SRC_NONE = 0
@@ -75,7 +76,22 @@ SIGNATURES = [
                                      C.POINTER(C.c_double)]),
     ("ns_adjoint_backward", C.c_int, [_VP, _VP]),
     ("ns_adjoint_context", C.c_int, [_VP, C.POINTER(_VP)]),
+    ("ns_read_dados", C.c_int, [C.c_char_p, _VP]),
+    ("ns_parse_dados", C.c_int, [C.c_char_p, _VP]),
+    ("ns_dados_grid", C.c_int, [_VP, C.c_int] + [_VP] * 8),
+    ("ns_dados_profiles", C.c_int, [_VP] * 6),
+    ("ns_create_dados", C.c_int, [_VP, C.c_int, C.c_int, C.c_int, C.POINTER(_VP)]),
+    ("ns_vorticity", C.c_int, [_VP, _VP]),
+    ("ns_write_contorno", C.c_int, [_VP, C.c_char_p, _VP, _VP]),
+    ("ns_format_real", C.c_int, [C.c_double, C.c_char_p, C.c_int]),
+    ("ns_probes_arm", C.c_int, [_VP, C.c_int, _VP, _VP, C.c_int]),
+    ("ns_probes_capture", C.c_int, [_VP]),
+    ("ns_probes_drain", C.c_int, [_VP, _VP, C.POINTER(C.c_int)]),
+    ("ns_run_euler", C.c_int, [C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int]),
 ]
+
+NS_RUN_NO_CONTORNO = 1
+NS_RUN_QUIET = 2
 
 NS_KC_COUNT = 11
 
@@ -96,6 +112,25 @@ class NsParams(C.Structure):
         ("n_pt", C.c_double), ("r0", C.c_double),
         ("m", _VP), ("n", _VP), ("meshx", _VP), ("meshy", _VP), ("sigmax", _VP),
         ("sigmay", _VP), ("rhob", _VP), ("psib", _VP), ("Ub", _VP), ("src_field", _VP),
+    ]
+
+
+class NsDados(C.Structure):
+    """Mirror of `ns_dados` (include/ns_gb300.h): the dados.in namelists."""
+
+    _fields_ = [
+        ("imax", C.c_int32), ("jmax", C.c_int32), ("maxit", C.c_int32), ("cgd", C.c_int32),
+        ("cfd", C.c_int32), ("ctd", C.c_int32), ("D", C.c_int32), ("iterw", C.c_int32),
+        ("num_procs_x", C.c_int32), ("num_procs_y", C.c_int32),
+        ("dt", C.c_double), ("sigmaf", C.c_double),
+        ("r0_acous", C.c_double), ("amplitude", C.c_double), ("m_pt_acous", C.c_double),
+        ("n_pt_acous", C.c_double), ("wfi", C.c_double), ("wff", C.c_double), ("wf", C.c_double),
+        ("pxfft", C.c_double * 5),
+        ("mmin", C.c_double), ("mmax", C.c_double), ("nmin", C.c_double), ("nmax", C.c_double),
+        ("pxr", C.c_double * 3), ("pyr", C.c_double * 3),
+        ("U1", C.c_double), ("U2", C.c_double), ("Re", C.c_double), ("Pr", C.c_double),
+        ("T1", C.c_double), ("T2", C.c_double), ("Tref", C.c_double),
+        ("c1b", C.c_double), ("c2b", C.c_double), ("c3b", C.c_double),
     ]
 
 

@@ -511,7 +511,9 @@ int ns_adjoint_create(const ns_params *p, int nobs, const double *obs_x, const d
     a->dudm0 = c->dudm;
     a->dudn0 = c->dudn;
     // base pressure (uniform p_b is required: the loss is on p - p_b)
-    a->pb = p->ub_layout == NS_LAYOUT_FORTRAN ? p->Ub[3] : p->Ub[3 * (size_t)p->imax * p->jmax];
+    a->pb = (p->ub_layout == NS_LAYOUT_FORTRAN || p->ub_layout == NS_LAYOUT_ROWS)
+                ? p->Ub[3]
+                : p->Ub[3 * (size_t)p->imax * p->jmax];
     std::vector<ns::adj::Obs> ob(nobs);
     const double x0 = p->m[0], y0 = p->n[0];
     for (int q = 0; q < nobs; q++) {

@@ -81,14 +81,16 @@ int cuda_err(ns_ctx *c, cudaError_t e, const char *what)
         if (e_ != cudaSuccess) return cuda_err((c), e_, #call);   \
     } while (0)
 
-// Per-line coefficient table (see ns::kCoefStride).
+// Per-line coefficient table (see ns::kCoefStride); mesh == NULL: no metric.
 void build_coef(std::vector<double> &tab, int n, double h, const double *mesh, int D,
                 int metric_mode)
 {
     tab.assign((size_t)n * ns::kCoefStride, 0.0);
     for (int q = 0; q < n; q++) {
         double mt = 1.0;
-        if (metric_mode == NS_METRIC_EVERYWHERE)
+        if (!mesh)
+            mt = 1.0;
+        else if (metric_mode == NS_METRIC_EVERYWHERE)
             mt = mesh[q];
         else if (q < D || q >= n - D)
             mt = mesh[q];
@@ -282,12 +284,14 @@ void free_all(ns_ctx *c)
     if (c->step_exec) cudaGraphExecDestroy(c->step_exec);
     double *bufs[] = {c->U,    c->U2,   c->W,     c->dudm, c->dudn, c->aux,
                       c->Ubase, c->src, c->xcoef, c->ycoef, c->sigx, c->sigy,
-                      c->rhob, c->psib, c->stage_sin, c->probe_buf};
+                      c->rhob, c->psib, c->stage_sin, c->probe_buf, c->rec_buf,
+                      c->vx, c->vy, c->omega};
     for (double *b : bufs)
         if (b) cudaFree(b);
     if (c->d_iter) cudaFree(c->d_iter);
     if (c->d_count) cudaFree(c->d_count);
     if (c->probe_idx) cudaFree(c->probe_idx);
+    if (c->rec_idx) cudaFree(c->rec_idx);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
 }
 
@@ -327,7 +331,8 @@ int validate(const ns_params *p)
         return set_err(nullptr, NS_ERR_PARAM, "gaussian source needs m, n and r0 != 0");
     if (p->source_mode == NS_SRC_FIELD && !p->src_field)
         return set_err(nullptr, NS_ERR_PARAM, "field source needs src_field");
-    if (p->ub_layout != NS_LAYOUT_FORTRAN && p->ub_layout != NS_LAYOUT_SOA)
+    if (p->ub_layout != NS_LAYOUT_FORTRAN && p->ub_layout != NS_LAYOUT_SOA &&
+        p->ub_layout != NS_LAYOUT_ROWS)
         return set_err(nullptr, NS_ERR_PARAM, "ub_layout=%d", p->ub_layout);
     return NS_OK;
 }
@@ -340,6 +345,12 @@ int upload_field(ns_ctx *c, const double *h, int layout, double *dplanes)
     if (layout == NS_LAYOUT_SOA) {
         NS_CUDA(c, cudaMemcpy2DAsync(dplanes, d.pitch * sizeof(double), h, row, row,
                                      (size_t)d.jmax * d.nk, cudaMemcpyHostToDevice, c->stream));
+    } else if (layout == NS_LAYOUT_ROWS) {
+        // rows of a field constant along i, expanded on the device
+        double *stage = (dplanes == c->U2) ? c->dudm : c->U2;
+        NS_CUDA(c, cudaMemcpyAsync(stage, h, (size_t)d.nk * d.jmax * sizeof(double),
+                                   cudaMemcpyHostToDevice, c->stream));
+        NS_CUDA(c, ns::launch_rows_to_planes(stage, dplanes, d, c->stream));
     } else if (layout == NS_LAYOUT_FORTRAN) {
         // stage the raw array in the scratch state buffer, then scatter
         double *stage = (dplanes == c->U2) ? c->dudm : c->U2;
@@ -360,6 +371,7 @@ int create_split(ns_ctx *c)
     ns::SplitState &sp = c->sp;
     const int imax = d.imax, jmax = d.jmax, nk = d.nk;
     auto ub = [&](int k, int i, int j) -> double {
+        if (p->ub_layout == NS_LAYOUT_ROWS) return p->Ub[k + (size_t)nk * j];
         return p->ub_layout == NS_LAYOUT_FORTRAN
                    ? p->Ub[k + (size_t)nk * (i + (size_t)imax * j)]
                    : p->Ub[((size_t)k * jmax + j) * imax + i];
@@ -464,6 +476,14 @@ int create_split(ns_ctx *c)
 }
 
 }  // namespace
+
+namespace ns {
+void build_line_coef(std::vector<double> &tab, int n, double h, const double *mesh, int D,
+                     int metric_mode)
+{
+    build_coef(tab, n, h, mesh, D, metric_mode);
+}
+}  // namespace ns
 
 namespace ns {
 void record_error(const char *msg) { g_last_error = msg; }

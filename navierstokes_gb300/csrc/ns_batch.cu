@@ -971,6 +971,7 @@ int ns_batch_create(const ns_params *const *params, int n, int precision, ns_bat
         const ns_params *p = params[q];
         const int imax = p->imax, jmax = p->jmax;
         auto ub = [&](int k, int i, int j) -> double {
+            if (p->ub_layout == NS_LAYOUT_ROWS) return p->Ub[k + 4 * (size_t)j];
             return p->ub_layout == NS_LAYOUT_FORTRAN ? p->Ub[k + 4 * ((size_t)i + (size_t)imax * j)]
                                                      : p->Ub[((size_t)k * jmax + j) * imax + i];
         };

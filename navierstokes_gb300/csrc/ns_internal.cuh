@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string>
+#include <vector>
 
 #include "../../include/ns_gb300.h"
 
@@ -44,6 +45,30 @@ constexpr int kCoefStride = 8;
 // Points per block of the FP64 filter recurrences (loads issued one block
 // ahead).
 constexpr int kFilterPf = 8;
+
+// ---------------------------------------------------------------------------
+// DRP first derivative along a line (diff.f90:40-238 with the metric of
+// diff.f90:276-350 folded into the coefficients).
+// f points at position q of a line of length n and stride st; c = the 8
+// coefficients of position q.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double dline(const double *__restrict__ f, long long st, int q,
+                                        int n, const double *__restrict__ c)
+{
+    if (q >= 3 && q < n - 3) {
+        const double c1 = c[4], c2 = c[5], c3 = c[6];
+        double r = c1 * (f[st] - f[-st]);
+        r = fma(c2, f[2 * st] - f[-2 * st], r);
+        r = fma(c3, f[3 * st] - f[-3 * st], r);
+        return r;
+    }
+    const int o0 = (q < 3) ? -q : (n - 7 - q);
+    const double *g = f + (long long)o0 * st;
+    double r = c[0] * g[0];
+#pragma unroll
+    for (int z = 1; z < 7; z++) r = fma(c[z], g[(long long)z * st], r);
+    return r;
+}
 
 // Filter coefficients pre-multiplied by the filter strength.
 struct FilterCoef {
@@ -108,6 +133,12 @@ struct ns_ctx {
     double *probe_buf = nullptr;
     int probe_cap = 0;
     int32_t *probe_idx = nullptr;
+    // probe recorder (ns_probes_*): rec_cap records of rec_npts*nk values
+    double *rec_buf = nullptr;
+    int32_t *rec_idx = nullptr;
+    int rec_cap = 0, rec_npts = 0, rec_n = 0;
+    // output path (ns_vorticity): metric-free derivative tables, omega plane
+    double *vx = nullptr, *vy = nullptr, *omega = nullptr;
     // host-side constants
     ns::Physics phys;
     ns::FilterCoef fx, fy;
@@ -139,6 +170,13 @@ cudaError_t launch_probes(const double *U, const Dims &d, int np, const int32_t 
                           double *out, cudaStream_t s);
 cudaError_t launch_count_nonfinite(const double *U, const Dims &d, unsigned long long *count,
                                    cudaStream_t s);
+// Per-line derivative table of kCoefStride doubles per position, 1/h and
+// the metric folded in (mesh == nullptr: no metric) (ns_api.cu).
+void build_line_coef(std::vector<double> &tab, int n, double h, const double *mesh, int D,
+                     int metric_mode);
+// NS_LAYOUT_ROWS: rows[k + nk*j] -> every point of row j of plane k (ns_output.cu)
+cudaError_t launch_rows_to_planes(const double *rows, double *planes, const Dims &d,
+                                  cudaStream_t s);
 int count_step_launches(const ns_ctx *c);
 // Makes msg the text ns_last_error(NULL) returns (ns_api.cu).
 void record_error(const char *msg);

@@ -22,30 +22,6 @@
 namespace ns {
 
 // ---------------------------------------------------------------------------
-// DRP first derivative along a line (diff.f90:40-238 with the metric of
-// diff.f90:276-350 folded into the coefficients).
-// f points at position q of a line of length n and stride st; c = the 8
-// coefficients of position q.
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ double dline(const double *__restrict__ f, long long st, int q,
-                                        int n, const double *__restrict__ c)
-{
-    if (q >= 3 && q < n - 3) {
-        const double c1 = c[4], c2 = c[5], c3 = c[6];
-        double r = c1 * (f[st] - f[-st]);
-        r = fma(c2, f[2 * st] - f[-2 * st], r);
-        r = fma(c3, f[3 * st] - f[-3 * st], r);
-        return r;
-    }
-    const int o0 = (q < 3) ? -q : (n - 7 - q);
-    const double *g = f + (long long)o0 * st;
-    double r = c[0] * g[0];
-#pragma unroll
-    for (int z = 1; z < 7; z++) r = fma(c[z], g[(long long)z * st], r);
-    return r;
-}
-
-// ---------------------------------------------------------------------------
 // k_prim: T and 1/rho (rhs.f90:20), pointwise.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_prim(Dims d, const double *__restrict__ U,

@@ -84,6 +84,10 @@ def lib():
                                     C.POINTER(C.c_double)]
         L.ora_init_dados.argtypes = [C.c_int, C.c_int, C.c_int] + [C.c_double] * 6 + [C.c_int] + \
             [C.c_void_p] * 6 + [C.POINTER(C.c_double)] * 2
+        L.ora_mixing_layer.argtypes = [C.c_int, C.c_void_p] + [C.c_double] * 4 + \
+            [C.c_void_p] * 4
+        L.ora_vorticity.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
+                                    C.c_void_p, C.c_void_p]
         L.ora_coeffs.argtypes = [C.c_int, C.c_void_p]
         L.ora_coeffs.restype = C.c_int
         L.ora_set_threads.argtypes = [C.c_int]
@@ -133,6 +137,24 @@ def init_dados(imax, jmax, D, mmin, mmax, nmin, nmax, c1b, c2b, quirk_buffer=Tru
                          out["sigmay"].ctypes.data, C.byref(dm), C.byref(dn))
     out["dm"], out["dn"] = dm.value, dn.value
     return out
+
+
+def mixing_layer(n, U1, U2, T1, T2):
+    """init.f90:359-373 -> uba, Tb, rhob, psib on the rows n."""
+    n = np.ascontiguousarray(n, dtype=np.float64)
+    out = [np.zeros(len(n)) for _ in range(4)]
+    lib().ora_mixing_layer(len(n), n.ctypes.data, U1, U2, T1, T2, *[o.ctypes.data for o in out])
+    return tuple(out)
+
+
+def vorticity(U, dm, dn):
+    """outt.f90:43-49 with diffall.f90's metric-free DRP: U is the memory of
+    U(nk,imax,jmax) shaped (jmax, imax, nk); returns omega (jmax, imax)."""
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    jmax, imax, nk = U.shape
+    om = np.zeros((jmax, imax))
+    lib().ora_vorticity(imax, jmax, nk, dm, dn, U.ctypes.data, om.ctypes.data)
+    return om
 
 
 class Oracle:

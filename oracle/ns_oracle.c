@@ -785,3 +785,71 @@ void ora_init_dados(int imax, int jmax, int D, double mmin, double mmax,
     *dm_out = dm;
     *dn_out = dn;
 }
+
+/* init_variables profiles, init.f90:359-373 (gamma = 1.4 at :361,
+ * deltamx = 0.4 at :358, psi1 = 1 and psi2 = 0 at :362-363). */
+void ora_mixing_layer(int jmax, const double *n, double U1, double U2,
+                      double T1, double T2, double *uba, double *Tb,
+                      double *rhob, double *psib)
+{
+    const double u1b = U1, u2b = U2, deltamx = 0.4, gamma = 1.4;
+    const double psi1 = 1.0, psi2 = 0.0;
+    int j;
+    for (j = 1; j <= jmax; j++) {
+        uba[j - 1] = 0.5 * (u1b + u2b + (u1b - u2b) * tanh(2.0 * n[j - 1] / deltamx));
+        Tb[j - 1] = T1 * (uba[j - 1] - u2b) / (u1b - u2b) + T2 * (u1b - uba[j - 1]) / (u1b - u2b) +
+                    (gamma - 1.0) / 2.0 * (u1b - uba[j - 1]) * (uba[j - 1] - u2b);
+        rhob[j - 1] = 1.0 / (Tb[j - 1]);
+        psib[j - 1] = 0.5 * (psi1 + psi2 + (psi1 - psi2) * tanh(2.0 * n[j - 1] / deltamx));
+    }
+}
+
+/* 1-based access into an (nn,imx,*) array with an explicit row length */
+#define A3x(a, nn, imx, k, i, j) \
+    (a)[((size_t)(k)-1) + (size_t)(nn) * (((size_t)(i)-1) + (size_t)(imx) * ((size_t)(j)-1))]
+
+/* diffall.f90 derivatives of variable k at (i,j): deropm (:5-43) dispatches
+ * to dudx (:45-64), dx4 (:66-106), dx5 (:108-150), dx6 (:152-193) with
+ * p = -1 at the right end (coefficients mirrored, summed from z = 7 down).
+ * Each term is (a*u)/h, summed left to right; no metric. */
+static double dall_point(const double *u, int nn, int k, int imax, int jmax, int i, int j,
+                         int along_y, double h)
+{
+    const int nq = along_y ? jmax : imax, q = along_y ? j : i;
+    const double *c;
+    int o0, z;
+    double r = 0.0;
+#define UQ(qq) (along_y ? A3x(u, nn, imax, k, i, (qq)) : A3x(u, nn, imax, k, (qq), j))
+    if (q >= 4 && q <= nq - 3) {
+        for (z = 1; z <= 3; z++) r = r + (a_dudx[z] * (UQ(q + z) - UQ(q - z))) / h;
+        return r;
+    }
+    if (q <= 3) {
+        /* dx6 (q=1, offsets 0..6), dx5 (q=2, -1..5), dx4 (q=3, -2..4) */
+        c = (q == 1) ? a_dudx6 : (q == 2) ? a_dudx5 : a_dudx4;
+        o0 = 1 - q;
+        for (z = 1; z <= 7; z++) r = r + c[z] * UQ(q + o0 + z - 1) / h;
+        return r;
+    }
+    /* right end: z = 7 down to 1 with the mirrored a(z) = a_dudx*b(z) */
+    c = (q == nq) ? a_dudx6b : (q == nq - 1) ? a_dudx5b : a_dudx4b;
+    o0 = (q == nq) ? -7 : (q == nq - 1) ? -6 : -5;
+    for (z = 7; z >= 1; z--) r = r + c[z] * UQ(q + z + o0) / h;
+    return r;
+#undef UQ
+}
+
+void ora_vorticity(int imax, int jmax, int nk, double dm, double dn,
+                   const double *U, double *omega)
+{
+    int j;
+#pragma omp parallel for schedule(static)
+    for (j = 1; j <= jmax; j++) {
+        int i;
+        for (i = 1; i <= imax; i++) {
+            const double dvdx = dall_point(U, nk, 3, imax, jmax, i, j, 0, dm);
+            const double dudy = dall_point(U, nk, 2, imax, jmax, i, j, 1, dn);
+            omega[(size_t)(i - 1) + (size_t)imax * (j - 1)] = dvdx - dudy;
+        }
+    }
+}

@@ -74,6 +74,17 @@ void ora_init_dados(int imax, int jmax, int D, double mmin, double mmax,
                     int quirk_buffer, double *m, double *n, double *meshx,
                     double *meshy, double *sigmax, double *sigmay,
                     double *dm, double *dn);
+/* Base-flow profiles of init_variables (init.f90:341-373): the tanh mixing
+ * layer uba, Tb, rhob = 1/Tb and psib on rows n[jmax], gamma = 1.4,
+ * deltamx = 0.4, psi1 = 1, psi2 = 0. */
+void ora_mixing_layer(int jmax, const double *n, double U1, double U2,
+                      double T1, double T2, double *uba, double *Tb,
+                      double *rhob, double *psib);
+/* Vorticity of the output path (outt.f90:43-49): the metric-free DRP
+ * derivatives of diffall.f90:5-380 on the whole grid, omega =
+ * dv/dx - du/dy, written omega[(i-1) + imax*(j-1)]. */
+void ora_vorticity(int imax, int jmax, int nk, double dm, double dn,
+                   const double *U, double *omega);
 /* Coefficient tables of the reference, for known-answer tests.
  * which: 0 a_dudx(3), 1 a_dudx4, 2 a_dudx5, 3 a_dudx6, 4 a_dudx4b,
  * 5 a_dudx5b, 6 a_dudx6b (7 each), 7 df(-6:6) (13), 8 dfb x (-1:5),
