@@ -214,6 +214,12 @@ NS_API const char *ns_kernel_name(int kernel_class);
  * FP64 stage kernels on GB300. */
 NS_API int ns_fp64_peak(int device, double *tflops);
 
+/* Library diagnostic, no counterpart in the reference: the exp (fn = 0),
+ * log (fn = 1) and 1/x (fn = 2) the stage kernels use for the transport law
+ * mu(T), k(T) (coefficients.f90:27-59), evaluated on device `device` for
+ * x[0..n) into y[0..n) (host arrays). */
+NS_API int ns_math_eval(int fn, const double *x, double *y, int n, int device);
+
 /*
  * Batched sweeps: many independent Euler instances (inviscid = 1, nk = 4,
  * base flow uniform in x with v = 0 and uniform p; each with its own size,

@@ -576,6 +576,13 @@ int ns_create(const ns_params *p, ns_ctx **out)
         NS_TRY(create_split(c));
         goto constants;
     }
+    if (c->visc) {
+        const cudaError_t me = ns::ensure_math_tables(c->dev);
+        if (me != cudaSuccess) {
+            rc = cuda_err(c, me, "transport-law tables");
+            goto fail;
+        }
+    }
     NS_TRY(dalloc(c, &c->U, nk * P));
     NS_TRY(dalloc(c, &c->U2, nk * P));
     NS_TRY(dalloc(c, &c->W, nk * P));

@@ -1,5 +1,8 @@
 // ns_diag.cu -- library diagnostics with no counterpart in the reference.
 //
+// ns_math_eval: the transport law's exp, log and 1/x (ns_fastmath.cuh) on
+// host arrays, for testing them against the library functions.
+//
 // ns_fp64_peak: the FP64 FMA throughput of a device, measured with a
 // register-only DFMA loop (8 independent chains per thread, 4 blocks of 256
 // threads per SM).  On GB300 the FP64 pipe, not HBM, bounds the FP64 stage
@@ -60,5 +63,22 @@ extern "C" int ns_fp64_peak(int device, double *tflops)
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     *tflops = best;
+    return rc;
+}
+
+extern "C" int ns_math_eval(int fn, const double *x, double *y, int n, int device)
+{
+    if (fn < 0 || fn > 2 || n < 0 || (n > 0 && (!x || !y))) return NS_ERR_PARAM;
+    if (n == 0) return NS_OK;
+    if (cudaSetDevice(device) != cudaSuccess) return NS_ERR_CUDA;
+    if (ns::ensure_math_tables(device) != cudaSuccess) return NS_ERR_CUDA;
+    double *d = nullptr;
+    if (cudaMalloc(&d, 2 * (size_t)n * sizeof(double)) != cudaSuccess) return NS_ERR_OOM;
+    int rc = NS_OK;
+    if (cudaMemcpy(d, x, (size_t)n * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
+        ns::launch_math_eval(fn, d, d + n, n, 0) != cudaSuccess ||
+        cudaMemcpy(y, d + n, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
+        rc = NS_ERR_CUDA;
+    cudaFree(d);
     return rc;
 }

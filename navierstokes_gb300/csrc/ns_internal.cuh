@@ -174,6 +174,10 @@ cudaError_t launch_count_nonfinite(const double *U, const Dims &d, unsigned long
 // the metric folded in (mesh == nullptr: no metric) (ns_api.cu).
 void build_line_coef(std::vector<double> &tab, int n, double h, const double *mesh, int D,
                      int metric_mode);
+// Tables of the transport-law exp/log (ns_kernels.cu): filled once per
+// device, outside stream capture.
+cudaError_t ensure_math_tables(int device);
+cudaError_t launch_math_eval(int fn, const double *x, double *y, int n, cudaStream_t s);
 // NS_LAYOUT_ROWS: rows[k + nk*j] -> every point of row j of plane k (ns_output.cu)
 cudaError_t launch_rows_to_planes(const double *rows, double *planes, const Dims &d,
                                   cudaStream_t s);

@@ -17,9 +17,56 @@
 //   k_filter<x>          lddfilterx as chunked recurrences  filtering.f90:9-96
 //   k_filter<y>          lddfiltery                         filtering.f90:98-190
 //   k_bc                 ccpml                              cc.f90:6-68
+#include <cmath>
+#include <mutex>
+
+#include "ns_fastmath.cuh"
 #include "ns_internal.cuh"
 
 namespace ns {
+
+cudaError_t ensure_math_tables(int device)
+{
+    static std::mutex mu;
+    static bool done[1024];
+    std::lock_guard<std::mutex> lock(mu);
+    if (device < 0 || device >= 1024) return cudaErrorInvalidDevice;
+    if (done[device]) return cudaSuccess;
+    fm::Tables t;
+    for (int j = 0; j < 64; j++) t.exp2j[j] = std::exp2(j / 64.0);
+    for (int j = 0; j < 128; j++) {
+        // 1/(1 + (j + 1/2)/128) rounded to 12 significant bits
+        const double c = std::ldexp(std::nearbyint(std::ldexp(1.0 / (1.0 + (j + 0.5) / 128.0), 12)), -12);
+        t.logc[j] = c;
+        t.lognc[j] = -std::log(c);
+    }
+    int cur = 0;
+    cudaError_t e = cudaGetDevice(&cur);
+    if (e == cudaSuccess && cur != device) e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(fm::g_tables, &t, sizeof t);
+    if (cur != device) cudaSetDevice(cur);
+    if (e == cudaSuccess) done[device] = true;
+    return e;
+}
+
+__global__ void k_math_eval(int fn, const double *__restrict__ x, double *__restrict__ y, int n)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    if (fn == 0) {
+        y[q] = fm::exp_t(x[q]);
+    } else {
+        double lg, rc;
+        fm::log_rcp_t(x[q], lg, rc);
+        y[q] = (fn == 1) ? lg : rc;
+    }
+}
+
+cudaError_t launch_math_eval(int fn, const double *x, double *y, int n, cudaStream_t s)
+{
+    k_math_eval<<<(n + 255) / 256, 256, 0, s>>>(fn, x, y, n);
+    return cudaGetLastError();
+}
 
 // ---------------------------------------------------------------------------
 // k_prim: T and 1/rho (rhs.f90:20), pointwise.
@@ -70,12 +117,12 @@ __global__ void __launch_bounds__(256)
         const double Tx = dline(fT, 1, i, d.imax, cx);
         const double Ty = dline(fT, st, j, d.jmax, cy);
         const double x = ph.Tref * T;
-        const double L = log(x);
-        const double y = 1.0 / x;
+        double L, y;
+        fm::log_rcp_t(x, L, y);  // log(x), 1/x
         const double amu = fma(ph.A_mi, L, fma(fma(ph.C_mi, y, ph.B_mi), y, ph.D_mi));
         const double ak = fma(ph.A_k, L, fma(fma(ph.C_k, y, ph.B_k), y, ph.D_k));
-        const double mu = ph.mu0inv * exp(amu);
-        const double kc = ph.k0inv * exp(ak);
+        const double mu = ph.mu0inv * fm::exp_t(amu);
+        const double kc = ph.k0inv * fm::exp_t(ak);
         aux[AUX_KTX * P + idx] = Tx * kc;  // kdT (derivs.f90:48-56)
         aux[AUX_KTY * P + idx] = Ty * kc;
         // TAU_IJ (eqeuler.f90:37-39)

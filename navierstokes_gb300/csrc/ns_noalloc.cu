@@ -219,6 +219,9 @@ extern "C" int ns_step_noalloc(const ns_params *p, double *U, int64_t pitch, int
         e = cudaGetSymbolAddress((void **)&ptr, g_noalloc_work);
         if (e != cudaSuccess || !ptr)
             return fail(NS_ERR_CUDA, "ns_step_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+        e = ns::ensure_math_tables(dev);
+        if (e != cudaSuccess)
+            return fail(NS_ERR_CUDA, "ns_step_noalloc: transport-law tables: %s", cudaGetErrorString(e));
         g_work_ptr[dev] = ptr;
     }
     cudaStream_t s = (cudaStream_t)stream;
