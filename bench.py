@@ -204,17 +204,22 @@ def run_reference(args, world, rank):
 
 
 # Algorithmic HBM bytes per point of one launch of the split-precision
-# kernels (nk = 4): stage reads q' (4 x FP32) and w (4 x FP64) and writes
-# both; each filter reads and writes q'.
-SPLIT_BYTES_PER_POINT = {"k_split_stage": 96, "k_split_filter_x": 32,
-                         "k_split_filter_y": 32}
-SPLIT_STEP_BYTES_MIN = 960   # per point-step: 6 x (96 + 2 x 32)
+# kernels: q' is 7 FP32 planes (rho'; u', v', p' hi; their lo parts) = 28 B;
+# the stage reads q' and w (4 x FP64) and writes both; each filter reads and
+# writes q'.
+SPLIT_BYTES_PER_POINT = {"k_split_stage": 120, "k_split_filter_x": 56,
+                         "k_split_filter_y": 56}
+SPLIT_STEP_BYTES_MIN = 1392   # per point-step: 6 x (120 + 2 x 56)
+# NS_PREC_SPLIT32: q' is 4 FP32 planes (16 B)
+SPLIT32_BYTES_PER_POINT = {"k_split_stage": 96, "k_split_filter_x": 32,
+                           "k_split_filter_y": 32}
 
 
 def split_study(args, local, hbm_peak):
     """Config-3 workload: Euler, 4096x4096 uniform grid, M = 0.5, pulse 1e-4,
-    vortex 1e-3, 1000 steps; split precision against plain FP64 (throughput
-    of both and p' = p - p_b error at steps 100/500/1000)."""
+    vortex 1e-3, 1000 steps; split precision (u', v', p' as FP32 pairs) and
+    the all-FP32 split against plain FP64 (throughput of each and p' = p - p_b
+    error at steps 100/500/1000)."""
     import ctypes as C
     import torch
     from navierstokes_gb300 import Solver, cases
@@ -227,7 +232,8 @@ def split_study(args, local, hbm_peak):
     rates = {}
     states = {}
     kernels = {}
-    for name, prec in (("fp64", L.NS_PREC_FP64), ("split", L.NS_PREC_SPLIT)):
+    for name, prec in (("fp64", L.NS_PREC_FP64), ("split", L.NS_PREC_SPLIT),
+                       ("split32", L.NS_PREC_SPLIT32)):
         s = Solver(case, device=local, precision=prec)
         s.set_stream(stream.cuda_stream)
         s.set_state(case.U0)
@@ -251,32 +257,41 @@ def split_study(args, local, hbm_peak):
         ms = e0.elapsed_time(e1) / args.steps
         rates[name] = {"value": case.points / (ms * 1e-3) / 1e6, "ms_per_step": ms,
                        "gpu_launches_per_step": s.launches_per_step()}
-        if name == "split":
+        if name in ("split", "split32"):
+            kernels = {} if name == "split" else kernels
             kms = (C.c_double * L.NS_KC_COUNT)()
             kn = (C.c_int * L.NS_KC_COUNT)()
             L.check(s.lib.ns_time_kernels(s._ctx, 20_000, 2, kms, kn), s._ctx)
             for k in range(L.NS_KC_COUNT):
                 if kn[k]:
                     kname = s.lib.ns_kernel_name(k).decode()
-                    bpp = SPLIT_BYTES_PER_POINT.get(kname)
-                    kernels[kname] = {"ms_per_launch": kms[k], "launches_per_step": kn[k]}
+                    bpp = (SPLIT_BYTES_PER_POINT if name == "split"
+                           else SPLIT32_BYTES_PER_POINT).get(kname)
+                    entry = {"ms_per_launch": kms[k], "launches_per_step": kn[k]}
                     if bpp:
                         gbs = bpp * case.points / (kms[k] * 1e-3) / 1e9
-                        kernels[kname]["achieved_gbs"] = gbs
-                        kernels[kname]["hbm_frac"] = gbs / hbm_peak
+                        entry["achieved_gbs"] = gbs
+                        entry["hbm_frac"] = gbs / hbm_peak
+                    if name == "split":
+                        kernels[kname] = entry
+                    else:
+                        rates[name].setdefault("kernels", {})[kname] = entry
         s.close()
     tot = sum(v["ms_per_launch"] * v["launches_per_step"] for v in kernels.values())
     for v in kernels.values():
         v["share"] = v["ms_per_launch"] * v["launches_per_step"] / tot
     dom = max(kernels, key=lambda n: kernels[n]["share"])
-    errs = {}
-    for n in args.split_error_steps:
-        a, b = states["fp64"][n], states["split"][n]
-        dp = b[..., 3] - a[..., 3]
-        pr = a[..., 3] - case.Ub[..., 3]
-        errs[str(n)] = {"p_rel_l2": float(np.linalg.norm(dp) / np.linalg.norm(pr)),
-                        "p_rel_max": float(np.max(np.abs(dp)) / np.max(np.abs(pr))),
-                        "p_abs_max": float(np.max(np.abs(dp)))}
+    def p_errors(mode):
+        errs = {}
+        for n in args.split_error_steps:
+            a, b = states["fp64"][n], states[mode][n]
+            dp = b[..., 3] - a[..., 3]
+            pr = a[..., 3] - case.Ub[..., 3]
+            errs[str(n)] = {"p_rel_l2": float(np.linalg.norm(dp) / np.linalg.norm(pr)),
+                            "p_rel_max": float(np.max(np.abs(dp)) / np.max(np.abs(pr))),
+                            "p_abs_max": float(np.max(np.abs(dp)))}
+        return errs
+    errs = p_errors("split")
     step_gbs = SPLIT_STEP_BYTES_MIN * case.points / (rates["split"]["ms_per_step"] * 1e-3) / 1e9
     out.update({"value": rates["split"]["value"], "unit": UNIT,
                 "fp64_value": rates["fp64"]["value"],
@@ -288,8 +303,14 @@ def split_study(args, local, hbm_peak):
                              "achieved": kernels[dom].get("achieved_gbs"),
                              "peak": hbm_peak, "unit": "GB/s",
                              "frac": kernels[dom].get("hbm_frac"),
-                             "step_frac_of_960B_per_point": step_gbs / hbm_peak},
-                "kernels": kernels})
+                             "step_frac_of_1392B_per_point": step_gbs / hbm_peak},
+                "kernels": kernels,
+                "split32": {"what": "every perturbation one FP32 number (NS_PREC_SPLIT32)",
+                            "value": rates["split32"]["value"], "unit": UNIT,
+                            "ms_per_step": rates["split32"]["ms_per_step"],
+                            "speedup_vs_fp64": rates["split32"]["value"] / rates["fp64"]["value"],
+                            "p_error_vs_fp64": p_errors("split32"),
+                            "kernels": rates["split32"].get("kernels")}})
     return out
 
 
@@ -307,7 +328,7 @@ def batch_study(args, local):
                        f"{pts} points in total, monopole sources, M ~ U[0,0.6], "
                        f"{args.batch_steps} steps", "points": pts}
     finals = {}
-    for name, prec in (("fp64", L.NS_PREC_FP64), ("split", L.NS_PREC_SPLIT)):
+    for name, prec in (("fp64", L.NS_PREC_FP64), ("split", L.NS_PREC_SPLIT32)):
         b = Batch(cs, device=local, precision=prec)
         stream = torch.cuda.Stream()
         b.set_stream(stream.cuda_stream)

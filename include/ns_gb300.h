@@ -60,9 +60,14 @@ enum {
 /* Arithmetic of the stage loop. */
 enum {
     NS_PREC_FP64 = 0,  /* plain FP64, the reference's arithmetic */
-    NS_PREC_SPLIT = 1  /* FP64 mean flow + FP32 perturbation state; Euler
-                          (inviscid = 1), nk = 4, base flow Ub uniform in x
-                          with v = 0 and uniform p */
+    NS_PREC_SPLIT = 1, /* FP64 mean flow + FP32 perturbation arithmetic;
+                          u', v', p' stored as FP32 hi + lo pairs, rho' as
+                          one FP32; Euler (inviscid = 1), nk = 4, base flow
+                          Ub uniform in x with v = 0 and uniform p */
+    NS_PREC_SPLIT32 = 2 /* the same with every perturbation one FP32 number
+                          (fewer bytes; the FP32 storage noise of u' drives
+                          p' near a strong vortex); the batched path's split
+                          mode */
 };
 
 /* Acoustic source of rk.f90:171-193. */

@@ -24,6 +24,7 @@ NS_LAYOUT_SOA = 1
 NS_LAYOUT_ROWS = 2
 NS_PREC_FP64 = 0
 NS_PREC_SPLIT = 1
+NS_PREC_SPLIT32 = 2
 NS_SRC_NONE = 0
 NS_SRC_GAUSSIAN = 1
 NS_SRC_FIELD = 2

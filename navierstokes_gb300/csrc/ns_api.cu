@@ -312,9 +312,10 @@ int validate(const ns_params *p)
         return set_err(nullptr, NS_ERR_PARAM, "D=%d: need 0 <= 2*D <= min(imax,jmax)", p->D);
     if (p->metric_mode != NS_METRIC_BANDS && p->metric_mode != NS_METRIC_EVERYWHERE)
         return set_err(nullptr, NS_ERR_PARAM, "metric_mode=%d", p->metric_mode);
-    if (p->precision != NS_PREC_FP64 && p->precision != NS_PREC_SPLIT)
+    if (p->precision != NS_PREC_FP64 && p->precision != NS_PREC_SPLIT &&
+        p->precision != NS_PREC_SPLIT32)
         return set_err(nullptr, NS_ERR_UNSUPPORTED, "precision=%d is not available", p->precision);
-    if (p->precision == NS_PREC_SPLIT && (!p->inviscid || p->nk != 4))
+    if (p->precision != NS_PREC_FP64 && (!p->inviscid || p->nk != 4))
         return set_err(nullptr, NS_ERR_UNSUPPORTED,
                        "split precision is implemented for the Euler equations (inviscid=1) "
                        "with nk=4; got inviscid=%d nk=%d", p->inviscid, p->nk);
@@ -394,7 +395,8 @@ int create_split(ns_ctx *c)
     int rc;
     if ((rc = dalloc(c, &c->U, nk * P)) || (rc = dalloc(c, &c->U2, nk * P)) ||
         (rc = dalloc(c, &c->W, nk * P)) || (rc = dalloc(c, &c->Ubase, nk * P)) ||
-        (rc = dalloc(c, &sp.q[0], 4 * FP)) || (rc = dalloc(c, &sp.q[1], 4 * FP)) ||
+        (rc = dalloc(c, &sp.q[0], (size_t)(4 + sp.np) * FP)) ||
+        (rc = dalloc(c, &sp.q[1], (size_t)(4 + sp.np) * FP)) ||
         (rc = dalloc(c, &sp.xc, (size_t)ns::kCoefStride * imax)) ||
         (rc = dalloc(c, &sp.yc, (size_t)ns::kCoefStride * jmax)) ||
         (rc = dalloc(c, &sp.xcl, (size_t)ns::kCoefStride * imax)) ||
@@ -406,8 +408,9 @@ int create_split(ns_ctx *c)
         (rc = dalloc(c, &c->d_count, 1)))
         return rc;
     if (p->source_mode != NS_SRC_NONE && (rc = dalloc(c, &sp.src, FP))) return rc;
-    cudaError_t e = cudaMemsetAsync(sp.q[0], 0, 4 * FP * sizeof(float), c->stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(sp.q[1], 0, 4 * FP * sizeof(float), c->stream);
+    cudaError_t e = cudaMemsetAsync(sp.q[0], 0, (4 + sp.np) * FP * sizeof(float), c->stream);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(sp.q[1], 0, (4 + sp.np) * FP * sizeof(float), c->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->W, 0, nk * P * sizeof(double), c->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->d_iter, 0, sizeof(int), c->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->stage_sin, 0, 8 * sizeof(double), c->stream);
@@ -471,7 +474,7 @@ int create_split(ns_ctx *c)
     sp.mean.du = sp.mean_buf + 3 * jmax;
     sp.mean.p = (float)pb;
     sp.mean.gamma = (float)p->gamma;
-    sp.p_bc = (float)(1.0 / p->gamma - pb);
+    sp.p_bc = 1.0 / p->gamma - pb;
     return NS_OK;
 }
 
@@ -565,7 +568,8 @@ int ns_create(const ns_params *p, ns_ctx **out)
     d.plane = (long long)d.pitch * d.jmax;
     c->visc = !p->inviscid;
     const size_t P = (size_t)d.plane, nk = (size_t)d.nk;
-    c->split = (p->precision == NS_PREC_SPLIT);
+    c->split = (p->precision == NS_PREC_SPLIT || p->precision == NS_PREC_SPLIT32);
+    c->sp.np = (p->precision == NS_PREC_SPLIT) ? 3 : 0;
 
 #define NS_TRY(x)                     \
     do {                              \
@@ -682,10 +686,13 @@ constants:
         if (c->visc) {
             // GET_COEFFICIENTS, coefficients.f90:78-79
             const double Tr = p->Tref;
-            const double k0 = std::exp(p->A_k * std::log(1.0 * Tr) + p->B_k / Tr + p->C_k / Tr / Tr + p->D_k);
-            const double mi0 = std::exp(p->A_mi * std::log(1.0 * Tr) + p->B_mi / Tr + p->C_mi / Tr / Tr + p->D_mi);
-            ph.mu0inv = 1.0 / mi0;
-            ph.k0inv = 1.0 / k0;
+            const double ak0 = p->A_k * std::log(1.0 * Tr) + p->B_k / Tr + p->C_k / Tr / Tr + p->D_k;
+            const double ami0 = p->A_mi * std::log(1.0 * Tr) + p->B_mi / Tr + p->C_mi / Tr / Tr + p->D_mi;
+            ph.mu0inv = 1.0 / std::exp(ami0);
+            ph.k0inv = 1.0 / std::exp(ak0);
+            // mu/mu0 = exp(arg(T) - arg(Tref)): the constant term absorbs 1/mu0
+            ph.D_mi_s = p->D_mi - ami0;
+            ph.D_k_s = p->D_k - ak0;
         }
         c->fx = make_filter(p->sigmaf, kDfbX);
         c->fy = make_filter(p->sigmaf, kDfbY);
@@ -702,7 +709,8 @@ constants:
         if (c->split) {
             // FP32 filters are bound by memory: aim at 32 resident warps per SM
             ns::SplitState &sp = c->sp;
-            sp.warm = filter_warmup_thresh(p->sigmaf, std::ldexp(1.0, -32));
+            // pairs carry ~48 bits: warm-up to 2^-50; single FP32 to 2^-32
+            sp.warm = filter_warmup_thresh(p->sigmaf, std::ldexp(1.0, sp.np ? -50 : -32));
             const int twarps = nsm * 32;
             const int xgroups = 4 * ((d.jmax + 31) / 32);
             sp.fx_chunks = choose_chunks(xgroups, d.imax, sp.warm, twarps);

@@ -844,15 +844,15 @@ cudaError_t launch_step(ns_batch *b, cudaStream_t s)
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
-    if (b->precision == NS_PREC_SPLIT)
+    if (b->precision == NS_PREC_SPLIT32)
         return b->ty == 8 ? launch_step_t<float, 8>(b, s) : launch_step_t<float, 16>(b, s);
     return b->ty == 8 ? launch_step_t<double, 8>(b, s) : launch_step_t<double, 16>(b, s);
 }
 
 size_t smem_for(int precision, int ty)
 {
-    const size_t es = precision == NS_PREC_SPLIT ? 4 : 8;
-    const int pw = precision == NS_PREC_SPLIT ? 32 : 16;
+    const size_t es = precision == NS_PREC_SPLIT32 ? 4 : 8;
+    const int pw = precision == NS_PREC_SPLIT32 ? 32 : 16;
     const size_t tile = 4 * (size_t)(ty + 6) * 38 * es;
     const size_t fx = (size_t)ns::batch::kWarps * 2 * 32 * (pw + 1) * es;
     return std::max(tile, fx);
@@ -874,7 +874,7 @@ int configure(ns_batch *b, int ty, int bps)
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, b->dev);
     b->ty = ty;
     b->smem = smem_for(b->precision, ty);
-    int maxb = b->precision == NS_PREC_SPLIT
+    int maxb = b->precision == NS_PREC_SPLIT32
                    ? (ty == 8 ? occupancy<float, 8>(b->smem) : occupancy<float, 16>(b->smem))
                    : (ty == 8 ? occupancy<double, 8>(b->smem) : occupancy<double, 16>(b->smem));
     if (maxb < 1) return berr(b, NS_ERR_CUDA, "ns_batch: the step kernel cannot be resident");
@@ -934,7 +934,11 @@ int ns_batch_create(const ns_params *const *params, int n, int precision, ns_bat
 {
     if (!out || !params || n < 1) return berr(nullptr, NS_ERR_PARAM, "ns_batch_create: bad argument");
     *out = nullptr;
-    if (precision != NS_PREC_FP64 && precision != NS_PREC_SPLIT)
+    if (precision == NS_PREC_SPLIT)
+        return berr(nullptr, NS_ERR_UNSUPPORTED,
+                    "ns_batch_create: the batched path carries single FP32 perturbations: "
+                    "use NS_PREC_SPLIT32");
+    if (precision != NS_PREC_FP64 && precision != NS_PREC_SPLIT32)
         return berr(nullptr, NS_ERR_PARAM, "ns_batch_create: precision");
     for (int q = 0; q < n; q++) {
         const ns_params *p = params[q];
@@ -956,7 +960,7 @@ int ns_batch_create(const ns_params *const *params, int n, int precision, ns_bat
     b->dev = params[0]->device;
     b->precision = precision;
     int rc = NS_OK;
-    const size_t es = precision == NS_PREC_SPLIT ? 4 : 8;
+    const size_t es = precision == NS_PREC_SPLIT32 ? 4 : 8;
     std::vector<ns::batch::Inst> hin(n);
     std::vector<double> xcd, ycd;
     std::vector<double> xc, yc, sx, sy, rbc, mrho, mu, mdrho, mdu, corr;
@@ -965,7 +969,7 @@ int ns_batch_create(const ns_params *const *params, int n, int precision, ns_bat
     long long qoff = 0, woff = 0, soff = 0;
     int xoff = 0, yoff = 0;
     double sigmaf = params[0]->sigmaf;
-    const int warm = warmup_len(sigmaf, precision == NS_PREC_SPLIT ? std::ldexp(1.0, -32)
+    const int warm = warmup_len(sigmaf, precision == NS_PREC_SPLIT32 ? std::ldexp(1.0, -32)
                                                                    : std::ldexp(1.0, -60));
     for (int q = 0; q < n && rc == NS_OK; q++) {
         const ns_params *p = params[q];
@@ -1175,7 +1179,7 @@ int ns_batch_create(const ns_params *const *params, int n, int precision, ns_bat
                     fld[(size_t)j * in.pitch + i] = v;
                 }
             cudaError_t e;
-            if (precision == NS_PREC_SPLIT) {
+            if (precision == NS_PREC_SPLIT32) {
                 std::vector<float> ff(fld.begin(), fld.end());
                 e = cudaMemcpy((float *)b->src + in.s_off, ff.data(), ff.size() * 4, cudaMemcpyHostToDevice);
             } else {
@@ -1284,7 +1288,7 @@ int ns_batch_set_state(ns_batch *b, int q, const double *U, int layout)
     }
     const dim3 blk(32, 8), grd((in.imax + 31) / 32, (in.jmax + 7) / 8);
     if (e == cudaSuccess) {
-        if (b->precision == NS_PREC_SPLIT)
+        if (b->precision == NS_PREC_SPLIT32)
             ns::batch::k_batch_from_full<float><<<grd, blk, 0, b->stream>>>(
                 stg, in.imax, in.jmax, in.pitch, b->drho + in.y_off, b->du + in.y_off,
                 b->hpmean[q], (float *)b->q[0] + in.q_off, in.pitch);
@@ -1309,7 +1313,7 @@ int ns_batch_get_state(ns_batch *b, int q, double *U, int layout)
     double *stg = b->stagebuf;
     double *raw = b->stagebuf + 4 * (size_t)in.pitch * in.jmax;
     const dim3 blk(32, 8), grd((in.imax + 31) / 32, (in.jmax + 7) / 8);
-    if (b->precision == NS_PREC_SPLIT)
+    if (b->precision == NS_PREC_SPLIT32)
         ns::batch::k_batch_to_full<float><<<grd, blk, 0, b->stream>>>(
             (float *)b->q[0] + in.q_off, in.imax, in.jmax, in.pitch, b->drho + in.y_off,
             b->du + in.y_off, b->hpmean[q], stg, in.pitch);
@@ -1387,7 +1391,7 @@ int ns_batch_autotune(ns_batch *b, int iter0, int reps, int *ty, int *blocks_per
     int it = iter0;
     for (int t : {8, 16}) {
         const size_t sm = smem_for(b->precision, t);
-        const int maxb = b->precision == NS_PREC_SPLIT
+        const int maxb = b->precision == NS_PREC_SPLIT32
                              ? (t == 8 ? occupancy<float, 8>(sm) : occupancy<float, 16>(sm))
                              : (t == 8 ? occupancy<double, 8>(sm) : occupancy<double, 16>(sm));
         for (int bps = 1; bps <= maxb; bps++) {
@@ -1456,7 +1460,7 @@ int ns_batch_barrier_test(ns_batch *b, int extra, long long spin_limit)
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     cudaError_t e;
-    if (b->precision == NS_PREC_SPLIT)
+    if (b->precision == NS_PREC_SPLIT32)
         e = b->ty == 8 ? cudaLaunchKernelEx(&cfg, ns::batch::k_batch_step<float, 8>, a)
                        : cudaLaunchKernelEx(&cfg, ns::batch::k_batch_step<float, 16>, a);
     else

@@ -83,6 +83,8 @@ struct Physics {
     double gamma, inv_re, inv_re_pr, gm1_re, dt, inv_pe, alpha_cond;
     double Tref, mu0inv, k0inv;
     double A_mi, B_mi, C_mi, D_mi, A_k, B_k, C_k, D_k;
+    // D_mi + log(mu0inv), D_k + log(k0inv): mu = exp(A ln x + B/x + C/x^2 + D_mi_s)
+    double D_mi_s, D_k_s;
 };
 
 struct StageCoef {
@@ -101,7 +103,11 @@ struct SplitMean {
 // Device state of the split-precision path (precision = NS_PREC_SPLIT).
 struct SplitState {
     int fpitch = 0;                   // FP32 row pitch (elements)
-    float *q[2] = {nullptr, nullptr}; // perturbation ping-pong, 4 planes each
+    // variables carried as hi + lo pairs: u', v', p' (3, NS_PREC_SPLIT) or none
+    // (0, NS_PREC_SPLIT32); a buffer holds 4 + np FP32 planes: rho', u', v',
+    // p', then the lo parts
+    int np = 3;
+    float *q[2] = {nullptr, nullptr}; // perturbation ping-pong
     float *xc = nullptr, *yc = nullptr;
     float *xcl = nullptr, *ycl = nullptr;  // FP64 table minus its FP32 rounding
     float *sigx = nullptr, *sigy = nullptr, *src = nullptr;
@@ -109,7 +115,7 @@ struct SplitState {
     float *ycorr = nullptr;           // [4][jmax]: y filter applied to Ub, minus Ub
     float *mean_buf = nullptr;        // rho, u, drho, du: [4][jmax]
     SplitMean mean{};
-    float p_bc = 0.f;                 // 1/gamma - p_b
+    double p_bc = 0.0;                // 1/gamma - p_b
     int warm = 0, fx_chunks = 1, fy_chunks = 1;
 };
 

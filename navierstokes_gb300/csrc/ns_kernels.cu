@@ -33,10 +33,10 @@ cudaError_t ensure_math_tables(int device)
     if (device < 0 || device >= 1024) return cudaErrorInvalidDevice;
     if (done[device]) return cudaSuccess;
     fm::Tables t;
-    for (int j = 0; j < 64; j++) t.exp2j[j] = std::exp2(j / 64.0);
-    for (int j = 0; j < 128; j++) {
-        // 1/(1 + (j + 1/2)/128) rounded to 12 significant bits
-        const double c = std::ldexp(std::nearbyint(std::ldexp(1.0 / (1.0 + (j + 0.5) / 128.0), 12)), -12);
+    for (int j = 0; j < 256; j++) t.exp2j[j] = std::exp2(j / 256.0);
+    for (int j = 0; j < 256; j++) {
+        // 1/(1 + (j + 1/2)/256) rounded to 12 significant bits
+        const double c = std::ldexp(std::nearbyint(std::ldexp(1.0 / (1.0 + (j + 0.5) / 256.0), 12)), -12);
         t.logc[j] = c;
         t.lognc[j] = -std::log(c);
     }
@@ -119,10 +119,11 @@ __global__ void __launch_bounds__(256)
         const double x = ph.Tref * T;
         double L, y;
         fm::log_rcp_t(x, L, y);  // log(x), 1/x
-        const double amu = fma(ph.A_mi, L, fma(fma(ph.C_mi, y, ph.B_mi), y, ph.D_mi));
-        const double ak = fma(ph.A_k, L, fma(fma(ph.C_k, y, ph.B_k), y, ph.D_k));
-        const double mu = ph.mu0inv * fm::exp_t(amu);
-        const double kc = ph.k0inv * fm::exp_t(ak);
+        // 1/mu0 and 1/k0 enter as log(1/mu0) + D, log(1/k0) + D (Physics)
+        const double amu = fma(ph.A_mi, L, fma(fma(ph.C_mi, y, ph.B_mi), y, ph.D_mi_s));
+        const double ak = fma(ph.A_k, L, fma(fma(ph.C_k, y, ph.B_k), y, ph.D_k_s));
+        const double mu = fm::exp_t(amu);
+        const double kc = fm::exp_t(ak);
         aux[AUX_KTX * P + idx] = Tx * kc;  // kdT (derivs.f90:48-56)
         aux[AUX_KTY * P + idx] = Ty * kc;
         // TAU_IJ (eqeuler.f90:37-39)

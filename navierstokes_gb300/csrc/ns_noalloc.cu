@@ -316,8 +316,12 @@ extern "C" int ns_step_noalloc(const ns_params *p, double *U, int64_t pitch, int
         ph.inv_re_pr = 1.0 / p->Re / p->Pr;
         ph.gm1_re = (p->gamma - 1.0) / p->Re;
         const double Tr = p->Tref;
-        ph.k0inv = 1.0 / std::exp(p->A_k * std::log(1.0 * Tr) + p->B_k / Tr + p->C_k / Tr / Tr + p->D_k);
-        ph.mu0inv = 1.0 / std::exp(p->A_mi * std::log(1.0 * Tr) + p->B_mi / Tr + p->C_mi / Tr / Tr + p->D_mi);
+        const double ak0 = p->A_k * std::log(1.0 * Tr) + p->B_k / Tr + p->C_k / Tr / Tr + p->D_k;
+        const double ami0 = p->A_mi * std::log(1.0 * Tr) + p->B_mi / Tr + p->C_mi / Tr / Tr + p->D_mi;
+        ph.k0inv = 1.0 / std::exp(ak0);
+        ph.mu0inv = 1.0 / std::exp(ami0);
+        ph.D_mi_s = p->D_mi - ami0;
+        ph.D_k_s = p->D_k - ak0;
     }
     c.fx = filter_coef(p->sigmaf, kDfbX);
     c.fy = filter_coef(p->sigmaf, kDfbY);

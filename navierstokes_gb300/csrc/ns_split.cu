@@ -11,6 +11,17 @@
 // not preserve constants (filtering.f90:114-120), acts on Ub by a fixed
 // FP64 amount that is precomputed per row and added back.
 //
+// With NP = 3 (NS_PREC_SPLIT) u', v' and p' are each carried as an
+// unevaluated sum of two FP32 numbers (hi + lo, about 48 significant bits);
+// rho' is a single FP32 number.  With NP = 0 (NS_PREC_SPLIT32) all four are
+// single FP32 numbers.  FP32 storage rounds every value three times per
+// stage; that noise random-walks at wavenumbers the selective filter does not
+// damp.  For a vortex with |u'| ~ 1e-3 next to an acoustic pulse it reached
+// ~35 ulps of u' after 300 steps and drove p' through the divergence to
+// 7e-10 (1e-4 of p'); the p' storage noise itself is the next floor (4e-11
+// after 1000 steps).  Planes of a perturbation buffer: 0 rho', 1 u', 2 v',
+// 3 p' (hi parts), then 3 + k the lo part of variable k = 1 .. NP.
+//
 // FP64 <-> FP32 conversions of the accumulator update are done with integer
 // bit operations (IEEE-754 layouts, round to nearest even): on GB300 the F2F
 // instructions run on the FP64 pipe, which is about 60x slower than FP32.
@@ -102,7 +113,32 @@ __device__ __forceinline__ void drp_ff(const float *fp, const float *fm, const f
     }
 }
 
-template <bool FIRST, bool SRC>
+// Variable k (0 rho', 1 u', 2 v', 3 p') is a hi + lo pair when 1 <= k <= NP.
+template <int NP>
+__device__ __forceinline__ constexpr bool is_pair(int k)
+{
+    return k >= 1 && k <= NP;
+}
+
+// (h, l) + a for a pair with |h| >= |l + a| (Fast2Sum): renormalised pair
+__device__ __forceinline__ void pair_add(float &h, float &l, float a)
+{
+    const float t = l + a;
+    const float nh = h + t;
+    l = t - (nh - h);
+    h = nh;
+}
+
+// (h, l) * s with the product's rounding error kept (FMA two-product)
+__device__ __forceinline__ void pair_scale(float &h, float &l, float s)
+{
+    const float p = h * s;
+    const float e = fmaf(h, s, -p);
+    l = fmaf(l, s, e);
+    h = p;
+}
+
+template <int NP, bool FIRST, bool SRC>
 __global__ void __launch_bounds__(256)
     k_split_stage(Dims d, int fpitch, const float *__restrict__ qin, float *__restrict__ qout,
                   double *__restrict__ W, const float *__restrict__ xc,
@@ -112,7 +148,8 @@ __global__ void __launch_bounds__(256)
                   const float *__restrict__ src, const double *__restrict__ stage_sin,
                   float dt, double alpha, double beta, int stage)
 {
-    __shared__ float sq[4][kSH][kSW];
+    constexpr int NPL = 4 + NP;
+    __shared__ float sq[NPL][kSH][kSW];
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int i0 = blockIdx.x * kTX, j0 = blockIdx.y * kTY;
     const long long fplane = (long long)fpitch * d.jmax;
@@ -138,7 +175,7 @@ __global__ void __launch_bounds__(256)
             const bool ok = rowok && gi >= 0 && gi < d.imax;
             const long long g = (long long)gj * fpitch + gi;
 #pragma unroll
-            for (int k = 0; k < 4; k++) sq[k][r][cc] = ok ? qin[k * fplane + g] : 0.f;
+            for (int k = 0; k < NPL; k++) sq[k][r][cc] = ok ? qin[k * fplane + g] : 0.f;
         }
     }
     __syncthreads();
@@ -146,6 +183,10 @@ __global__ void __launch_bounds__(256)
     if (i >= d.imax) return;
     const float *cxp = xc + kCoefStride * i;
     const float cx4 = cxp[4], cx5 = cxp[5], cx6 = cxp[6];
+    // the FP64 coefficients minus their FP32 roundings: without them every
+    // derivative is scaled by 1 + O(6e-8) and advection runs that much off
+    const float *cxlp = xcl + kCoefStride * i;
+    const float clx4 = cxlp[4], clx5 = cxlp[5], clx6 = cxlp[6];
     const bool xint = (i >= 3 && i < d.imax - 3);
 #pragma unroll
     for (int h = 0; h < 2; h++) {
@@ -155,23 +196,34 @@ __global__ void __launch_bounds__(256)
         const long long fidx = (long long)j * fpitch + i;
         const long long didx = (long long)j * d.pitch + i;
         const int sr = ly + kH, sc = tx + kH;
-        float q[4], gx[4], gy[4];
+        float q[NPL], gx[NPL], gy[NPL];
         const float *cyp = yc + kCoefStride * j;
         const bool yint = (j >= 3 && j < d.jmax - 3);
 #pragma unroll
-        for (int k = 0; k < 4; k++) {
+        const float *cylp = ycl + kCoefStride * j;
+        for (int k = 0; k < NPL; k++) {
             q[k] = sq[k][sr][sc];
             if (xint) {
-                float r = cx4 * (sq[k][sr][sc + 1] - sq[k][sr][sc - 1]);
-                r = fmaf(cx5, sq[k][sr][sc + 2] - sq[k][sr][sc - 2], r);
-                gx[k] = fmaf(cx6, sq[k][sr][sc + 3] - sq[k][sr][sc - 3], r);
+                const float d1 = sq[k][sr][sc + 1] - sq[k][sr][sc - 1];
+                const float d2 = sq[k][sr][sc + 2] - sq[k][sr][sc - 2];
+                const float d3 = sq[k][sr][sc + 3] - sq[k][sr][sc - 3];
+                float r = 0.f;
+                if (k < 4) r = fmaf(clx6, d3, fmaf(clx5, d2, clx4 * d1));
+                r = fmaf(cx4, d1, r);
+                r = fmaf(cx5, d2, r);
+                gx[k] = fmaf(cx6, d3, r);
             } else {
                 gx[k] = closure_f32(qin + k * fplane + fidx, 1, i, d.imax, cxp);
             }
             if (yint) {
-                float r = cyp[4] * (sq[k][sr + 1][sc] - sq[k][sr - 1][sc]);
-                r = fmaf(cyp[5], sq[k][sr + 2][sc] - sq[k][sr - 2][sc], r);
-                gy[k] = fmaf(cyp[6], sq[k][sr + 3][sc] - sq[k][sr - 3][sc], r);
+                const float d1 = sq[k][sr + 1][sc] - sq[k][sr - 1][sc];
+                const float d2 = sq[k][sr + 2][sc] - sq[k][sr - 2][sc];
+                const float d3 = sq[k][sr + 3][sc] - sq[k][sr - 3][sc];
+                float r = 0.f;
+                if (k < 4) r = fmaf(cylp[6], d3, fmaf(cylp[5], d2, cylp[4] * d1));
+                r = fmaf(cyp[4], d1, r);
+                r = fmaf(cyp[5], d2, r);
+                gy[k] = fmaf(cyp[6], d3, r);
             } else {
                 gy[k] = closure_f32(qin + k * fplane + fidx, fpitch, j, d.jmax, cyp);
             }
@@ -188,19 +240,25 @@ __global__ void __launch_bounds__(256)
                 const float fmx[3] = {sq[1][sr][sc - 1], sq[1][sr][sc - 2], sq[1][sr][sc - 3]};
                 const float fpy[3] = {sq[2][sr + 1][sc], sq[2][sr + 2][sc], sq[2][sr + 3][sc]};
                 const float fmy[3] = {sq[2][sr - 1][sc], sq[2][sr - 2][sc], sq[2][sr - 3][sc]};
-                const float chx[3] = {cx4, cx5, cx6}, clx[3] = {xcl[kCoefStride * i + 4],
-                                                                xcl[kCoefStride * i + 5],
-                                                                xcl[kCoefStride * i + 6]};
+                const float chx[3] = {cx4, cx5, cx6}, clx[3] = {clx4, clx5, clx6};
                 const float chy[3] = {cyp[4], cyp[5], cyp[6]},
-                            cly[3] = {ycl[kCoefStride * j + 4], ycl[kCoefStride * j + 5],
-                                      ycl[kCoefStride * j + 6]};
+                            cly[3] = {cylp[4], cylp[5], cylp[6]};
                 float xh, xl, yh, yl, sh, se;
                 drp_ff(fpx, fmx, chx, clx, xh, xl);
                 drp_ff(fpy, fmy, chy, cly, yh, yl);
                 two_sum(xh, yh, sh, se);
+                // the lo parts' derivatives are small: plain FP32 is exact enough
                 div = sh + (se + (xl + yl));
+                if (NP >= 2) div += gx[NP >= 2 ? 4 : 0] + gy[NP >= 2 ? 5 : 0];
             } else {
                 div = gx[1] + gy[2];
+                if (NP >= 2) div += gx[NP >= 2 ? 4 : 0] + gy[NP >= 2 ? 5 : 0];
+            }
+            // derivatives of the pair variables including their lo parts
+#pragma unroll
+            for (int k = 1; k <= NP; k++) {
+                gx[k] += gx[k + 3];
+                gy[k] += gy[k + 3];
             }
             // U = Ub + q'; dUb/dx = 0, v_b = 0, dp_b = 0 (eqeuler.f90:63-92, 1/Re = 0)
             const float rho = mean.rho[j] + q[0];
@@ -231,28 +289,35 @@ __global__ void __launch_bounds__(256)
             t = fmaf(gp, div, t);
             if (SRC) t = t - (float)stage_sin[stage] * src[fidx];
             r[3] = -t;
-            // rk_steep (rk.f90:163-164): FP64 accumulator
+            // rk_steep (rk.f90:163-164): FP64 accumulator; u', v' kept as pairs
 #pragma unroll
             for (int k = 0; k < 4; k++) {
                 const double dr = f2d_exact(dt * r[k]);
                 const double w = FIRST ? dr : fma(alpha, wold[h][k], dr);
                 W[k * d.plane + didx] = w;
-                q[k] = d2f_rn(fma(beta, w, f2d_exact(q[k])));
+                if (is_pair<NP>(k)) {
+                    float &lo = q[is_pair<NP>(k) ? k + 3 : k];
+                    const double v = fma(beta, w, f2d_exact(q[k]) + f2d_exact(lo));
+                    const float hi = d2f_rn(v);
+                    lo = d2f_rn(v - f2d_exact(hi));
+                    q[k] = hi;
+                } else {
+                    q[k] = d2f_rn(fma(beta, w, f2d_exact(q[k])));
+                }
             }
         }
         // bufferxy (rk.f90:77-151): U - Ub = q'
-        if (j < d.D || j >= d.jmax - d.D) {
-            const float s = sigy[j];
+        auto damp = [&](float s) {
 #pragma unroll
-            for (int k = 0; k < 4; k++) q[k] *= s;
-        }
-        if (i < d.D || i >= d.imax - d.D) {
-            const float s = sigx[i];
+            for (int k = 0; k < 4; k++) {
+                if (is_pair<NP>(k)) pair_scale(q[k], q[is_pair<NP>(k) ? k + 3 : k], s);
+                else q[k] *= s;
+            }
+        };
+        if (j < d.D || j >= d.jmax - d.D) damp(sigy[j]);
+        if (i < d.D || i >= d.imax - d.D) damp(sigx[i]);
 #pragma unroll
-            for (int k = 0; k < 4; k++) q[k] *= s;
-        }
-#pragma unroll
-        for (int k = 0; k < 4; k++) qout[k * fplane + fidx] = q[k];
+        for (int k = 0; k < NPL; k++) qout[k * fplane + fidx] = q[k];
     }
 }
 
@@ -306,9 +371,141 @@ __device__ __forceinline__ float passb_f(const float *w, int p, const FiltF &f)
     return fmaf(f.bm1, w[p - DIR] - u0, u0 + acc);
 }
 
+// The same two forms on hi + lo pairs (u', v'): the differences are
+// (h_s - h_0) + (l_s - l_0), the correction acc is FP32 (it is small), and
+// the result (h_0 + l_0) + acc is renormalised into a pair.
+__device__ __forceinline__ void pass2_p(const float *wh, const float *wl, const FiltF &f,
+                                        float &oh, float &ol)
+{
+    const float h0 = wh[6], l0 = wl[6];
+#define NS_DD(t) ((wh[t] - h0) + (wl[t] - l0))
+    float acc = f.m[6] * (NS_DD(12) + NS_DD(0));
+    acc = fmaf(f.m[5], NS_DD(11) + NS_DD(1), acc);
+    acc = fmaf(f.m[4], NS_DD(10) + NS_DD(2), acc);
+    acc = fmaf(f.m[3], NS_DD(9) + NS_DD(3), acc);
+    acc = fmaf(f.m[2], NS_DD(8) + NS_DD(4), acc);
+    acc = fmaf(f.m[1], NS_DD(7), acc);
+    acc = fmaf(f.m[1], NS_DD(5), acc);
+#undef NS_DD
+    oh = h0;
+    ol = l0;
+    pair_add(oh, ol, acc);
+}
+
+template <int DIR>
+__device__ __forceinline__ void passb_p(const float *wh, const float *wl, int p, const FiltF &f,
+                                        float &oh, float &ol)
+{
+    const float h0 = wh[p], l0 = wl[p];
+    float acc = fmaf(f.bsum, l0, f.bsum * h0);
+#pragma unroll
+    for (int z = 1; z <= 5; z++)
+        acc = fmaf(f.b[z], (wh[p + DIR * z] - h0) + (wl[p + DIR * z] - l0), acc);
+    acc = fmaf(f.bm1, (wh[p - DIR] - h0) + (wl[p - DIR] - l0), acc);
+    oh = h0;
+    ol = l0;
+    pair_add(oh, ol, acc);
+}
+
+// One filter line along y (stride st) of a single FP32 variable (PAIR =
+// false) or of a hi/lo pair (lo at sl).  Steps a .. b-1 of pass 2 with the
+// chunking of the FP64 kernel; cr: the FP64 action on the base flow, added
+// to every output.
+template <bool PAIR>
+__device__ __forceinline__ void filter_y_line(const float *__restrict__ s,
+                                              const float *__restrict__ sl, float *__restrict__ o,
+                                              float *__restrict__ ol, long long st, int n, int a,
+                                              int b, bool first, bool last, int q0, const FiltF &f,
+                                              const float *__restrict__ cr)
+{
+    float wh[13], wl[13];
+    auto put = [&](int pos, float h, float l) {
+        if (PAIR) {
+            pair_add(h, l, cr[pos]);
+            o[(long long)pos * st] = h;
+            ol[(long long)pos * st] = l;
+        } else {
+            o[(long long)pos * st] = h + cr[pos];
+        }
+    };
+#pragma unroll
+    for (int t = 0; t < 13; t++) {
+        wh[t] = s[(long long)(q0 - 6 + t) * st];
+        wl[t] = PAIR ? sl[(long long)(q0 - 6 + t) * st] : 0.f;
+    }
+    int q = q0;
+    if (first) {
+        // pass 1 from the true line start (q0 = 6)
+#pragma unroll
+        for (int p = 1; p <= 6; p++) {
+            if (PAIR) passb_p<1>(wh, wl, p, f, wh[p], wl[p]);
+            else wh[p] = passb_f<1>(wh, p, f);
+        }
+        if (a == 6) {
+#pragma unroll
+            for (int p = 0; p < 6; p++) put(p, wh[p], wl[p]);
+        }
+    }
+    // loads run eight steps ahead through a register ring (static indices by
+    // unrolling); the value appended at step q is position q+7
+    float ph[8], pl[8];
+#pragma unroll
+    for (int t = 0; t < 8; t++) {
+        const bool ok = q + 7 + t < n;
+        ph[t] = ok ? s[(long long)(q + 7 + t) * st] : 0.f;
+        pl[t] = (PAIR && ok) ? sl[(long long)(q + 7 + t) * st] : 0.f;
+    }
+    auto step = [&](int qq, float nh, float nl) {
+        float vh, vl = 0.f;
+        if (PAIR) pass2_p(wh, wl, f, vh, vl);
+        else vh = pass2_f(wh, f);
+        if (qq >= a) put(qq, vh, vl);
+#pragma unroll
+        for (int u = 0; u < 5; u++) {
+            wh[u] = wh[u + 1];
+            wl[u] = wl[u + 1];
+        }
+        wh[5] = vh;
+        wl[5] = vl;
+#pragma unroll
+        for (int u = 6; u < 12; u++) {
+            wh[u] = wh[u + 1];
+            wl[u] = wl[u + 1];
+        }
+        wh[12] = nh;
+        wl[12] = nl;
+    };
+    for (; q + 8 <= b; q += 8) {
+#pragma unroll
+        for (int t = 0; t < 8; t++) {
+            const int qq = q + t;
+            step(qq, ph[t], pl[t]);
+            const bool ok = qq + 15 < n;
+            ph[t] = ok ? s[(long long)(qq + 15) * st] : 0.f;
+            pl[t] = (PAIR && ok) ? sl[(long long)(qq + 15) * st] : 0.f;
+        }
+    }
+    for (; q < b; q++) {
+        const bool ok = q + 7 < n;
+        step(q, ok ? s[(long long)(q + 7) * st] : 0.f,
+             (PAIR && ok) ? sl[(long long)(q + 7) * st] : 0.f);
+    }
+    if (last) {
+        // pass 3: w[0..11] = positions n-12 .. n-1
+#pragma unroll
+        for (int x = 10; x >= 5; x--) {
+            if (PAIR) passb_p<-1>(wh, wl, x, f, wh[x], wl[x]);
+            else wh[x] = passb_f<-1>(wh, x, f);
+        }
+#pragma unroll
+        for (int x = 5; x < 12; x++) put(n - 12 + x, wh[x], wl[x]);
+    }
+}
+
 // y filter: thread per (column, variable, chunk); lanes on consecutive
 // columns, so each step reads and writes one coalesced row segment.
 // corr[k*jmax + j] is the FP64 action of the filter on the base flow.
+template <int NP>
 __global__ void __launch_bounds__(128)
     k_split_filter_y(Dims d, int fpitch, const float *__restrict__ src, float *__restrict__ dst,
                      int chunks, int warm, FiltF f, const float *__restrict__ corr)
@@ -320,81 +517,132 @@ __global__ void __launch_bounds__(128)
     const int rest = (int)(gid / d.imax);
     const int k = rest % 4, c = rest / 4;
     const int n = d.jmax;
-    const long long st = fpitch;
-    const long long base = (long long)k * fpitch * d.jmax + line;
-    const float *__restrict__ s = src + base;
-    float *__restrict__ o = dst + base;
-    const float *__restrict__ cr = corr + (long long)k * d.jmax;
+    const long long st = fpitch, fplane = (long long)fpitch * d.jmax;
+    const long long base = (long long)k * fplane + line;
+    const long long lbase = (long long)(k + 3) * fplane + line;  // lo plane of a pair
     const int len2 = n - 12;
     const int a = 6 + (int)(((long long)c * len2) / chunks);
     const int b = 6 + (int)(((long long)(c + 1) * len2) / chunks);
-    float w[13];
-    int q;
-    if (c == 0 || warm < 0 || a - warm <= 6) {
-#pragma unroll
-        for (int t = 0; t < 13; t++) w[t] = s[t * st];
-#pragma unroll
-        for (int p = 1; p <= 6; p++) w[p] = passb_f<1>(w, p, f);
-        if (c == 0) {
-#pragma unroll
-            for (int p = 0; p < 6; p++) o[p * st] = w[p] + cr[p];
-        }
-        q = 6;
-    } else {
-        q = a - warm;
-#pragma unroll
-        for (int t = 0; t < 13; t++) w[t] = s[(long long)(q - 6 + t) * st];
-    }
-    // steps q .. b-1; the value appended at step q is s[q+7].  Loads run
-    // eight steps ahead through a register ring (static indices by unrolling).
-    float pre[8];
-#pragma unroll
-    for (int t = 0; t < 8; t++) pre[t] = (q + 7 + t < n) ? s[(long long)(q + 7 + t) * st] : 0.f;
-    for (; q + 8 <= b; q += 8) {
-#pragma unroll
-        for (int t = 0; t < 8; t++) {
-            const int qq = q + t;
-            const float v = pass2_f(w, f);
-            if (qq >= a) o[(long long)qq * st] = v + cr[qq];
-#pragma unroll
-            for (int u = 0; u < 5; u++) w[u] = w[u + 1];
-            w[5] = v;
-#pragma unroll
-            for (int u = 6; u < 12; u++) w[u] = w[u + 1];
-            w[12] = pre[t];
-            pre[t] = (qq + 15 < n) ? s[(long long)(qq + 15) * st] : 0.f;
-        }
-    }
-    for (int t = 0; q < b; q++, t++) {
-        const float v = pass2_f(w, f);
-        if (q >= a) o[(long long)q * st] = v + cr[q];
-#pragma unroll
-        for (int u = 0; u < 5; u++) w[u] = w[u + 1];
-        w[5] = v;
-#pragma unroll
-        for (int u = 6; u < 12; u++) w[u] = w[u + 1];
-        w[12] = (q + 7 < n) ? s[(long long)(q + 7) * st] : 0.f;
-    }
-    if (c == chunks - 1) {
-#pragma unroll
-        for (int x = 10; x >= 5; x--) w[x] = passb_f<-1>(w, x, f);
-#pragma unroll
-        for (int x = 5; x < 12; x++) o[(long long)(n - 12 + x) * st] = w[x] + cr[n - 12 + x];
-    }
+    const bool exact = (c == 0 || warm < 0 || a - warm <= 6);
+    const int q0 = exact ? 6 : a - warm;
+    const float *cr = corr + (long long)k * d.jmax;
+    if (is_pair<NP>(k))
+        filter_y_line<true>(src + base, src + lbase, dst + base, dst + lbase, st, n, a, b, exact,
+                            c == chunks - 1, q0, f, cr);
+    else
+        filter_y_line<false>(src + base, nullptr, dst + base, nullptr, st, n, a, b, exact,
+                             c == chunks - 1, q0, f, cr);
 }
 
 // x filter: each warp owns 32 consecutive rows of one variable and one
 // chunk.  The old values a lane appends to its window (position q+7 at step
 // q) are staged 32 positions at a time through a [32][33] tile loaded with
-// coalesced row reads; the outputs go back the same way.
-constexpr int kXW = 4;  // warps per block
+// coalesced row reads; the outputs go back the same way.  Pair variables
+// stage their lo parts through a second pair of tiles.
+// warps per block: 4 for single FP32 variables, 2 when the lo tiles exist
+template <int NP>
+constexpr int x_warps()
+{
+    return NP ? 2 : 4;
+}
 
-__global__ void __launch_bounds__(32 * kXW)
+template <bool PAIR>
+__device__ __forceinline__ void filter_x_rows(const float *__restrict__ sbase,
+                                              const float *__restrict__ slbase,
+                                              float *__restrict__ obase, float *__restrict__ olbase,
+                                              int fpitch, int n, int nrows, int lane, int a, int b,
+                                              bool exact, bool first, bool last, int q0,
+                                              const FiltF &f, float (*ti)[33], float (*to)[33],
+                                              float (*til)[33], float (*tol)[33])
+{
+    const bool active = lane < nrows;
+    const long long roff = (long long)(active ? lane : 0) * fpitch;
+    const float *__restrict__ s = sbase + roff;
+    const float *__restrict__ sl = PAIR ? slbase + roff : nullptr;
+    float wh[13], wl[13];
+#pragma unroll
+    for (int t = 0; t < 13; t++) {
+        wh[t] = s[q0 - 6 + t];
+        wl[t] = PAIR ? sl[q0 - 6 + t] : 0.f;
+    }
+    if (exact) {
+#pragma unroll
+        for (int p = 1; p <= 6; p++) {
+            if (PAIR) passb_p<1>(wh, wl, p, f, wh[p], wl[p]);
+            else wh[p] = passb_f<1>(wh, p, f);
+        }
+        if (first && active)
+            for (int p = 0; p < 6; p++) {
+                obase[(long long)lane * fpitch + p] = wh[p];
+                if (PAIR) olbase[(long long)lane * fpitch + p] = wl[p];
+            }
+    }
+    // Steps q = q0 .. b-1 in blocks of 32: block B covers steps
+    // [q0+32B, q0+32B+32), appends positions q+7, writes outputs at q.
+    for (int qb = q0; qb < b; qb += 32) {
+        const int pin = qb + 7;  // first appended position of the block
+        for (int r = 0; r < nrows; r++) {
+            const int pos = pin + lane;
+            ti[r][lane] = (pos < n) ? sbase[(long long)r * fpitch + pos] : 0.f;
+            if (PAIR) til[r][lane] = (pos < n) ? slbase[(long long)r * fpitch + pos] : 0.f;
+        }
+        __syncwarp();
+        const int nstep = min(32, b - qb);
+        for (int t = 0; t < nstep; t++) {
+            float vh, vl = 0.f;
+            if (PAIR) pass2_p(wh, wl, f, vh, vl);
+            else vh = pass2_f(wh, f);
+            to[lane][t] = vh;
+            if (PAIR) tol[lane][t] = vl;
+#pragma unroll
+            for (int u = 0; u < 5; u++) {
+                wh[u] = wh[u + 1];
+                wl[u] = wl[u + 1];
+            }
+            wh[5] = vh;
+            wl[5] = vl;
+#pragma unroll
+            for (int u = 6; u < 12; u++) {
+                wh[u] = wh[u + 1];
+                wl[u] = wl[u + 1];
+            }
+            wh[12] = ti[lane][t];
+            wl[12] = PAIR ? til[lane][t] : 0.f;
+        }
+        __syncwarp();
+        // write outputs q = qb .. qb+nstep-1 that this chunk owns (q >= a)
+        for (int r = 0; r < nrows; r++) {
+            const int qq = qb + lane;
+            if (lane < nstep && qq >= a) {
+                obase[(long long)r * fpitch + qq] = to[r][lane];
+                if (PAIR) olbase[(long long)r * fpitch + qq] = tol[r][lane];
+            }
+        }
+        __syncwarp();
+    }
+    if (last && active) {
+        // w[0..11] = positions n-12 .. n-1 (pass 3)
+#pragma unroll
+        for (int x = 10; x >= 5; x--) {
+            if (PAIR) passb_p<-1>(wh, wl, x, f, wh[x], wl[x]);
+            else wh[x] = passb_f<-1>(wh, x, f);
+        }
+        for (int x = 5; x < 12; x++) {
+            obase[(long long)lane * fpitch + (n - 12 + x)] = wh[x];
+            if (PAIR) olbase[(long long)lane * fpitch + (n - 12 + x)] = wl[x];
+        }
+    }
+}
+
+template <int NP>
+__global__ void __launch_bounds__(32 * x_warps<NP>())
     k_split_filter_x(Dims d, int fpitch, const float *__restrict__ src, float *__restrict__ dst,
                      int chunks, int warm, FiltF f)
 {
-    __shared__ float tin[kXW][32][33];
-    __shared__ float tout[kXW][32][33];
+    constexpr int kXW = x_warps<NP>();
+    constexpr int kXL = NP ? kXW : 1;  // lo tiles only when pairs exist
+    __shared__ float tin[kXW][32][33], tout[kXW][32][33];
+    __shared__ float tinl[kXL][32][33], toutl[kXL][32][33];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int rows32 = (d.jmax + 31) / 32;
     const long long gw = (long long)blockIdx.x * kXW + wid;  // global warp
@@ -407,148 +655,125 @@ __global__ void __launch_bounds__(32 * kXW)
     const int row0 = rg * 32;
     const int nrows = min(32, d.jmax - row0);
     const long long fplane = (long long)fpitch * d.jmax;
-    const float *__restrict__ sbase = src + k * fplane + (long long)row0 * fpitch;
-    float *__restrict__ obase = dst + k * fplane + (long long)row0 * fpitch;
-    const bool active = lane < nrows;
-    const float *__restrict__ s = sbase + (long long)(active ? lane : 0) * fpitch;
-    float(*ti)[33] = tin[wid];
-    float(*to)[33] = tout[wid];
-
+    const long long roff = (long long)row0 * fpitch;
     const int len2 = n - 12;
     const int a = 6 + (int)(((long long)c * len2) / chunks);
     const int b = 6 + (int)(((long long)(c + 1) * len2) / chunks);
     const bool exact = (c == 0 || warm < 0 || a - warm <= 6);
     const int q0 = exact ? 6 : a - warm;
-
-    float w[13];
-    if (exact) {
-#pragma unroll
-        for (int t = 0; t < 13; t++) w[t] = s[t];
-#pragma unroll
-        for (int p = 1; p <= 6; p++) w[p] = passb_f<1>(w, p, f);
-        if (c == 0 && active)
-            for (int p = 0; p < 6; p++) obase[(long long)lane * fpitch + p] = w[p];
-    } else {
-#pragma unroll
-        for (int t = 0; t < 13; t++) w[t] = s[q0 - 6 + t];
-    }
-    // Steps q = q0 .. b-1 in blocks of 32: block B covers steps
-    // [q0+32B, q0+32B+32), appends positions q+7, writes outputs at q.
-    for (int qb = q0; qb < b; qb += 32) {
-        const int pin = qb + 7;  // first appended position of the block
-        // stage appended positions pin .. pin+31 (clipped to n)
-        for (int r = 0; r < nrows; r++) {
-            const int pos = pin + lane;
-            ti[r][lane] = (pos < n) ? sbase[(long long)r * fpitch + pos] : 0.f;
-        }
-        __syncwarp();
-        const int nstep = min(32, b - qb);
-        for (int t = 0; t < nstep; t++) {
-            const float v = pass2_f(w, f);
-            to[lane][t] = v;
-#pragma unroll
-            for (int u = 0; u < 5; u++) w[u] = w[u + 1];
-            w[5] = v;
-#pragma unroll
-            for (int u = 6; u < 12; u++) w[u] = w[u + 1];
-            w[12] = ti[lane][t];
-        }
-        __syncwarp();
-        // write outputs q = qb .. qb+nstep-1 that this chunk owns (q >= a)
-        for (int r = 0; r < nrows; r++) {
-            const int qq = qb + lane;
-            if (lane < nstep && qq >= a) obase[(long long)r * fpitch + qq] = to[r][lane];
-        }
-        __syncwarp();
-    }
-    if (c == chunks - 1 && active) {
-        // w[0..11] = positions n-12 .. n-1 (pass 3)
-#pragma unroll
-        for (int x = 10; x >= 5; x--) w[x] = passb_f<-1>(w, x, f);
-        for (int x = 5; x < 12; x++) obase[(long long)lane * fpitch + (n - 12 + x)] = w[x];
-    }
+    if (is_pair<NP>(k))
+        filter_x_rows<true>(src + k * fplane + roff, src + (k + 3) * fplane + roff,
+                            dst + k * fplane + roff, dst + (k + 3) * fplane + roff, fpitch, n,
+                            nrows, lane, a, b, exact, c == 0, c == chunks - 1, q0, f, tin[wid],
+                            tout[wid], tinl[NP ? wid : 0], toutl[NP ? wid : 0]);
+    else
+        filter_x_rows<false>(src + k * fplane + roff, nullptr, dst + k * fplane + roff, nullptr,
+                             fpitch, n, nrows, lane, a, b, exact, c == 0, c == chunks - 1, q0, f,
+                             tin[wid], tout[wid], tinl[0], toutl[0]);
 }
 
 // ---------------------------------------------------------------------------
 // ccpml (cc.f90:6-68) on q': rho'(1,j) = rhob(j) - rho_b(j), v' = 0,
-// p' = 1/gamma - p_b on every edge; extrapolations are the same in q'.
+// p' = 1/gamma - p_b on every edge; extrapolations are the same in q'.  The
+// perimeter is small, so values are combined in FP64 (u', v' as hi + lo).
 // ---------------------------------------------------------------------------
+template <int NP>
+__device__ __forceinline__ double bc_get(const float *q, long long P, int k, long long idx)
+{
+    double v = (double)q[k * P + idx];
+    if (is_pair<NP>(k)) v += (double)q[(k + 3) * P + idx];
+    return v;
+}
+
+template <int NP>
+__device__ __forceinline__ void bc_put(float *q, long long P, int k, long long idx, double v)
+{
+    const float h = (float)v;
+    q[k * P + idx] = h;
+    if (is_pair<NP>(k)) q[(k + 3) * P + idx] = (float)(v - (double)h);
+}
+
+template <int NP>
 __global__ void k_split_bc(Dims d, int fpitch, float *__restrict__ q,
-                           const float *__restrict__ rho_bc, float p_bc)
+                           const float *__restrict__ rho_bc, double p_bc)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const long long P = (long long)fpitch * d.jmax;
-    auto colval = [&](int i, int j, float *v) {
+    auto colval = [&](int i, int j, double *v) {
         const long long r = (long long)j * fpitch;
         if (i == 0) {
             v[0] = rho_bc[j];
-            v[1] = 2.f * q[P + r + 1] - q[P + r + 2];
-            v[2] = 0.f;
+            v[1] = 2.0 * bc_get<NP>(q, P, 1, r + 1) - bc_get<NP>(q, P, 1, r + 2);
+            v[2] = 0.0;
             v[3] = p_bc;
         } else {
             const int a = d.imax - 2, b = d.imax - 3;
-            for (int k = 0; k < 3; k++) v[k] = 2.f * q[k * P + r + a] - q[k * P + r + b];
+            for (int k = 0; k < 3; k++) v[k] = 2.0 * bc_get<NP>(q, P, k, r + a) - bc_get<NP>(q, P, k, r + b);
             v[3] = p_bc;
         }
     };
-    float v[4];
+    double v[4];
     if (t > 0 && t < d.jmax - 1) {
         const long long r = (long long)t * fpitch;
         colval(0, t, v);
-        for (int k = 0; k < 4; k++) q[k * P + r] = v[k];
+        for (int k = 0; k < 4; k++) bc_put<NP>(q, P, k, r, v[k]);
         colval(d.imax - 1, t, v);
-        for (int k = 0; k < 4; k++) q[k * P + r + d.imax - 1] = v[k];
+        for (int k = 0; k < 4; k++) bc_put<NP>(q, P, k, r + d.imax - 1, v[k]);
     }
     if (t < d.imax) {
         const int jt = d.jmax - 1;
-        float a[4], b[4];
+        double a[4], b[4];
         if (t == 0 || t == d.imax - 1) {
             colval(t, jt - 1, a);
             colval(t, jt - 2, b);
         } else {
             for (int k = 0; k < 4; k++) {
-                a[k] = q[k * P + (long long)(jt - 1) * fpitch + t];
-                b[k] = q[k * P + (long long)(jt - 2) * fpitch + t];
+                a[k] = bc_get<NP>(q, P, k, (long long)(jt - 1) * fpitch + t);
+                b[k] = bc_get<NP>(q, P, k, (long long)(jt - 2) * fpitch + t);
             }
         }
-        for (int k = 0; k < 3; k++) q[k * P + (long long)jt * fpitch + t] = 2.f * a[k] - b[k];
-        q[3 * P + (long long)jt * fpitch + t] = p_bc;
+        for (int k = 0; k < 3; k++) bc_put<NP>(q, P, k, (long long)jt * fpitch + t, 2.0 * a[k] - b[k]);
+        bc_put<NP>(q, P, 3, (long long)jt * fpitch + t, p_bc);
         if (t == 0 || t == d.imax - 1) {
             colval(t, 1, a);
             colval(t, 2, b);
         } else {
             for (int k = 0; k < 4; k++) {
-                a[k] = q[k * P + (long long)1 * fpitch + t];
-                b[k] = q[k * P + (long long)2 * fpitch + t];
+                a[k] = bc_get<NP>(q, P, k, (long long)1 * fpitch + t);
+                b[k] = bc_get<NP>(q, P, k, (long long)2 * fpitch + t);
             }
         }
-        for (int k = 0; k < 3; k++) q[k * P + t] = 2.f * a[k] - b[k];
-        q[3 * P + t] = p_bc;
+        for (int k = 0; k < 3; k++) bc_put<NP>(q, P, k, t, 2.0 * a[k] - b[k]);
+        bc_put<NP>(q, P, 3, t, p_bc);
     }
 }
 
-// State conversion: q' = f32(U - Ub) and U = Ub + q'.
+// State conversion: q' = U - Ub (pairs as hi + lo) and U = Ub + q'.
+template <int NP>
 __global__ void k_split_from_full(Dims d, int fpitch, const double *__restrict__ U,
                                   const double *__restrict__ Ub, float *__restrict__ q)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= d.imax || j >= d.jmax) return;
+    const long long P = (long long)fpitch * d.jmax, fi = (long long)j * fpitch + i;
     for (int k = 0; k < 4; k++) {
         const long long di = k * d.plane + (long long)j * d.pitch + i;
-        q[(long long)k * fpitch * d.jmax + (long long)j * fpitch + i] = (float)(U[di] - Ub[di]);
+        bc_put<NP>(q, P, k, fi, U[di] - Ub[di]);
     }
 }
 
+template <int NP>
 __global__ void k_split_to_full(Dims d, int fpitch, const float *__restrict__ q,
                                 const double *__restrict__ Ub, double *__restrict__ U)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= d.imax || j >= d.jmax) return;
+    const long long P = (long long)fpitch * d.jmax, fi = (long long)j * fpitch + i;
     for (int k = 0; k < 4; k++) {
         const long long di = k * d.plane + (long long)j * d.pitch + i;
-        U[di] = Ub[di] + (double)q[(long long)k * fpitch * d.jmax + (long long)j * fpitch + i];
+        U[di] = Ub[di] + bc_get<NP>(q, P, k, fi);
     }
 }
 
@@ -571,7 +796,8 @@ static FiltF to_f32(const FilterCoef &c)
     return f;
 }
 
-cudaError_t launch_split_kernel(ns_ctx *c, int cls, int stage, cudaStream_t s)
+template <int NP>
+static cudaError_t launch_split_np(ns_ctx *c, int cls, int stage, cudaStream_t s)
 {
     const Dims &d = c->d;
     SplitState &sp = c->sp;
@@ -583,11 +809,9 @@ cudaError_t launch_split_kernel(ns_ctx *c, int cls, int stage, cudaStream_t s)
         const dim3 blk(kTX, 8), grd((d.imax + kTX - 1) / kTX, (d.jmax + kTY - 1) / kTY);
         const bool src = sp.src != nullptr;
 #define NS_SPL(FIRST, SRC)                                                                      \
-    k_split_stage<FIRST, SRC><<<grd, blk, 0, s>>>(d, sp.fpitch, qa, qb, c->W, sp.xc, sp.yc,    \
-                                                  sp.xcl, sp.ycl, sp.mean, sp.sigx, sp.sigy,   \
-                                                  sp.src,                                      \
-                                                  c->stage_sin, (float)c->p.dt, c->alpha[stage], \
-                                                  c->beta[stage], stage)
+    k_split_stage<NP, FIRST, SRC><<<grd, blk, 0, s>>>(                                          \
+        d, sp.fpitch, qa, qb, c->W, sp.xc, sp.yc, sp.xcl, sp.ycl, sp.mean, sp.sigx, sp.sigy,    \
+        sp.src, c->stage_sin, (float)c->p.dt, c->alpha[stage], c->beta[stage], stage)
         if (stage == 0) {
             if (src) NS_SPL(true, true); else NS_SPL(true, false);
         } else {
@@ -598,19 +822,20 @@ cudaError_t launch_split_kernel(ns_ctx *c, int cls, int stage, cudaStream_t s)
     }
     case NS_KC_SPLIT_FX: {
         const long long warps = (long long)((d.jmax + 31) / 32) * 4 * sp.fx_chunks;
-        k_split_filter_x<<<(unsigned)((warps + kXW - 1) / kXW), 32 * kXW, 0, s>>>(
+        constexpr int kXW = x_warps<NP>();
+        k_split_filter_x<NP><<<(unsigned)((warps + kXW - 1) / kXW), 32 * kXW, 0, s>>>(
             d, sp.fpitch, qb, qa, sp.fx_chunks, sp.warm, to_f32(c->fx));
         break;
     }
     case NS_KC_SPLIT_FY: {
         const long long t = (long long)d.imax * 4 * sp.fy_chunks;
-        k_split_filter_y<<<(unsigned)((t + 127) / 128), 128, 0, s>>>(
+        k_split_filter_y<NP><<<(unsigned)((t + 127) / 128), 128, 0, s>>>(
             d, sp.fpitch, qa, qb, sp.fy_chunks, sp.warm, to_f32(c->fy), sp.ycorr);
         break;
     }
     case NS_KC_SPLIT_BC: {
         const int nt = d.imax > d.jmax ? d.imax : d.jmax;
-        k_split_bc<<<(nt + 127) / 128, 128, 0, s>>>(d, sp.fpitch, qb, sp.rho_bc, sp.p_bc);
+        k_split_bc<NP><<<(nt + 127) / 128, 128, 0, s>>>(d, sp.fpitch, qb, sp.rho_bc, sp.p_bc);
         break;
     }
     default:
@@ -619,17 +844,29 @@ cudaError_t launch_split_kernel(ns_ctx *c, int cls, int stage, cudaStream_t s)
     return cudaGetLastError();
 }
 
+cudaError_t launch_split_kernel(ns_ctx *c, int cls, int stage, cudaStream_t s)
+{
+    return c->sp.np == 3 ? launch_split_np<3>(c, cls, stage, s)
+                         : launch_split_np<0>(c, cls, stage, s);
+}
+
 cudaError_t launch_split_from_full(ns_ctx *c, const double *U, cudaStream_t s)
 {
     const dim3 blk(32, 8), grd((c->d.imax + 31) / 32, (c->d.jmax + 7) / 8);
-    k_split_from_full<<<grd, blk, 0, s>>>(c->d, c->sp.fpitch, U, c->Ubase, c->sp.q[0]);
+    if (c->sp.np == 3)
+        k_split_from_full<3><<<grd, blk, 0, s>>>(c->d, c->sp.fpitch, U, c->Ubase, c->sp.q[0]);
+    else
+        k_split_from_full<0><<<grd, blk, 0, s>>>(c->d, c->sp.fpitch, U, c->Ubase, c->sp.q[0]);
     return cudaGetLastError();
 }
 
 cudaError_t launch_split_to_full(ns_ctx *c, double *U, cudaStream_t s)
 {
     const dim3 blk(32, 8), grd((c->d.imax + 31) / 32, (c->d.jmax + 7) / 8);
-    k_split_to_full<<<grd, blk, 0, s>>>(c->d, c->sp.fpitch, c->sp.q[0], c->Ubase, U);
+    if (c->sp.np == 3)
+        k_split_to_full<3><<<grd, blk, 0, s>>>(c->d, c->sp.fpitch, c->sp.q[0], c->Ubase, U);
+    else
+        k_split_to_full<0><<<grd, blk, 0, s>>>(c->d, c->sp.fpitch, c->sp.q[0], c->Ubase, U);
     return cudaGetLastError();
 }
 

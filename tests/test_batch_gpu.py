@@ -39,7 +39,7 @@ def test_batch_split_matches_single_split(nslib):
     from navierstokes_gb300 import Batch
     cs = small_sweep(n=4, seed=5)
     nsteps = 40
-    with Batch(cs, precision=L.NS_PREC_SPLIT) as b:
+    with Batch(cs, precision=L.NS_PREC_SPLIT32) as b:
         b.set_initial()
         b.step(0, nsteps)
         b.synchronize()
@@ -54,7 +54,7 @@ def test_batch_split_matches_single_split(nslib):
 def test_batch_autotune_and_info(nslib):
     from navierstokes_gb300 import Batch
     cs = small_sweep(n=6, seed=7)
-    with Batch(cs, precision=L.NS_PREC_SPLIT) as b:
+    with Batch(cs, precision=L.NS_PREC_SPLIT32) as b:
         b.set_initial()
         ty, bps, ms = b.autotune(0, 1)
         assert ty in (8, 16) and bps >= 1 and ms > 0
@@ -77,3 +77,10 @@ def test_batch_barrier_timeout_is_reported_and_recoverable(nslib):
         after = b.get_state(1)
     ref = single(cs[1], 3, L.NS_PREC_FP64)
     assert_parity(after, ref, cs[1].Ub, label="after timeout")
+
+
+def test_batch_split_mode_is_fp32(nslib):
+    from navierstokes_gb300 import Batch
+    with pytest.raises(L.NsError) as e:
+        Batch(small_sweep(n=2), precision=L.NS_PREC_SPLIT)
+    assert e.value.code == L.NS_ERR_UNSUPPORTED
