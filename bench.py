@@ -443,6 +443,53 @@ def cpu_baseline_sample(case, seconds=20.0):
                       f"untimed step, C oracle (-O3, OpenMP over lines)"}
 
 
+def cpu_configs_study(seconds=8.0):
+    """The C oracle on every configuration's workload, on all host cores and
+    on one core: a bounded sample of steps each (the per-step rate is what
+    is reported).  Configuration 4 times its 64 instances one after the
+    other; configuration 5 times the forward step of the source problem."""
+    import oracle
+    from navierstokes_gb300 import cases
+    from navierstokes_gb300.adjoint import SourceProblem
+    oracle.build()
+    allc = os.cpu_count() or 1
+    work = [("1: 201x201 Euler pulse", [cases.acoustic_pulse_case()]),
+            ("2: 4096x2048 Navier-Stokes", [cases.stretched_ns_case()]),
+            ("3: 4096x4096 Euler, pulse + vortex", [cases.uniform_flow_case()]),
+            ("4: 64 Euler instances (seed 0)", cases.sweep_cases(n=64, seed=0)),
+            ("5: 512x512 Euler with source field", [SourceProblem(steps=10).case])]
+    out = {}
+    for name, cs in work:
+        row = {}
+        for threads in (allc, 1):
+            oracle.set_threads(threads)
+            # size the sample on one step of the first grid
+            o = oracle.Oracle(cs[0])
+            U = cs[0].U0.copy()
+            t0 = time.perf_counter()
+            o.run(U, 0, 1)
+            t1 = time.perf_counter() - t0
+            o.close()
+            per_case = t1 * sum(c.points for c in cs) / cs[0].points
+            n = max(1, min(50, int(seconds / max(per_case, 1e-4))))
+            pts = 0
+            t0 = time.perf_counter()
+            for c in cs:
+                o = oracle.Oracle(c)
+                U = c.U0.copy()
+                o.run(U, 0, n)
+                o.close()
+                pts += c.points * n
+            dt = time.perf_counter() - t0
+            row[f"{threads}_cores" if threads > 1 else "1_core"] = {
+                "value": pts / dt / 1e6, "steps_sampled": n}
+        out[name] = row
+    oracle.set_threads(allc)
+    return {"unit": UNIT, "cores": allc, "kind": "port",
+            "sample": "C oracle (-O3, OpenMP over lines), a few steps of each workload",
+            "configs": out}
+
+
 def run_ours(args, world, rank, local, pg):
     import torch
     from navierstokes_gb300 import Solver
@@ -575,6 +622,13 @@ def run_ours(args, world, rank, local, pg):
         except Exception as e:
             adjoint = {"failed": str(e)}
 
+    cpu_configs = None
+    if rank == 0 and world == 1 and args.cpu_configs:
+        try:
+            cpu_configs = cpu_configs_study()
+        except Exception as e:
+            cpu_configs = {"failed": str(e)}
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
@@ -604,6 +658,8 @@ def run_ours(args, world, rank, local, pg):
             line["batched"] = batched
         if adjoint is not None:
             line["adjoint"] = adjoint
+        if cpu_configs is not None:
+            line["cpu_configs"] = cpu_configs
         print(json.dumps(line), flush=True)
 
 
@@ -626,6 +682,8 @@ def main():
     ap.add_argument("--batch-steps", type=int, default=300)
     ap.add_argument("--no-adjoint", action="store_true",
                     help="skip the discrete-adjoint (config-5) study")
+    ap.add_argument("--cpu-configs", action="store_true",
+                    help="also time the C oracle on every configuration (all cores, 1 core)")
     ap.add_argument("--adjoint-steps", type=int, default=2000)
     ap.add_argument("--adjoint-k", type=int, default=100)
     ap.add_argument("--split-error-steps", type=lambda t: [int(x) for x in t.split(",")],
