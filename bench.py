@@ -45,14 +45,14 @@ BYTES_PER_POINT = {"k_prim": 32, "k_first": 144, "k_update": 240, "k_filter_x": 
 # FP64 work per grid point of one launch, from the ncu instruction counts of
 # profiles/fp64_counts_ns_2048x2048.md (nk = 4, Navier-Stokes): flops (2 per
 # DFMA, 1 per DADD/DMUL) and FP64-pipe thread instructions.
-FP64_FLOP_PER_POINT = {"k_prim": 12.0, "k_first": 219.15, "k_update": 111.45,
-                       "k_filter_x": 86.71, "k_filter_y": 86.71}
-FP64_INST_PER_POINT = {"k_prim": 7.0, "k_first": 142.03, "k_update": 74.82,
-                       "k_filter_x": 56.33, "k_filter_y": 56.33}
+FP64_FLOP_PER_POINT = {"k_prim": 12.0, "k_first": 166.15, "k_update": 111.45,
+                       "k_filter_x": 90.15, "k_filter_y": 90.15}
+FP64_INST_PER_POINT = {"k_prim": 7.0, "k_first": 112.03, "k_update": 74.82,
+                       "k_filter_x": 58.56, "k_filter_y": 58.56}
 # DRAM bytes (read + write) per point of one launch from the same capture
 # (2048x2048), scaled to a launch by the number of points.
-TRAFFIC_PER_POINT = {"k_prim": 21.4, "k_first": 130.8, "k_update": 230.6,
-                     "k_filter_x": 59.5, "k_filter_y": 59.5}
+TRAFFIC_PER_POINT = {"k_prim": 21.3, "k_first": 130.4, "k_update": 230.6,
+                     "k_filter_x": 61.8, "k_filter_y": 61.8}
 FP64_PEAK_FALLBACK_TFLOPS = 1.19  # DFMA throughput measured on the GB300s
 STEP_BYTES_FUSED_MIN = 1536  # compulsory bytes per point-step of a fused FP64 design, nk = 4
 
