@@ -154,6 +154,21 @@ def dist_setup(args):
     return world, rank, local, pg
 
 
+def max_over_ranks(pg, x, device="cpu"):
+    """The largest x over all ranks: the slowest replica's time."""
+    if pg is None:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(world, points, steps, seconds):
+    """Mpt-steps/s of the whole job: every replica's points over the slowest."""
+    return world * points * steps / seconds / 1e6
+
+
 def run_reference(args, world, rank):
     """CPU oracle on all host threads; rank 0 only."""
     if rank != 0:
@@ -528,13 +543,9 @@ def run_ours(args, world, rank, local, pg):
     torch.cuda.synchronize()
     barrier()
     clocks = sampler.stop()
-    ms = ev0.elapsed_time(ev1)
-    if pg is not None:
-        t = torch.tensor([ms], device=f"cuda:{local}")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(pg, ev0.elapsed_time(ev1), f"cuda:{local}")
     ms_step = ms / args.steps
-    value = world * case.points * args.steps / (ms * 1e-3) / 1e6
+    value = whole_job_rate(world, case.points, args.steps, ms * 1e-3)
 
     # ---- per-kernel device times (events around each launch) ---------------
     import ctypes as C
@@ -593,12 +604,8 @@ def run_ours(args, world, rank, local, pg):
     t0 = time.perf_counter()
     for k in range(args.steps):
         solver.rk_euler(Uh, (k + 1) * case.dt, k)
-    t_e2e = time.perf_counter() - t0
-    if pg is not None:
-        t = torch.tensor([t_e2e], device=f"cuda:{local}")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        t_e2e = float(t.item())
-    e2e_val = world * case.points * args.steps / t_e2e / 1e6
+    t_e2e = max_over_ranks(pg, time.perf_counter() - t0, f"cuda:{local}")
+    e2e_val = whole_job_rate(world, case.points, args.steps, t_e2e)
     nbytes = case.state_bytes()
 
     split = None
