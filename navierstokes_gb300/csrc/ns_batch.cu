@@ -57,6 +57,7 @@ struct Args {
     float fm_f[7], fbm1_f[2], fb_f[2][6], fbsum_f[2];
     double fm_d[7], fbm1_d[2], fb_d[2][6], fbsum_d[2];
     unsigned *bar_count, *bar_gen;
+    unsigned *work;            // per stage: next x-line item, next y-line item
     int *err;
     unsigned nblocks;          // blocks that take part in each barrier
     long long spin_limit;
@@ -409,16 +410,31 @@ __device__ void fy_item(const Args &a, int4 item, const T *srcq, T *dstq)
 #pragma unroll
         for (int t = 0; t < 13; t++) w[t] = s[(long long)(q - 6 + t) * st];
     }
-    for (; q < b0; q++) {
+    auto step = [&](int qq, T next) {
         const T v = pass2<T>(w, fc.m);
-        if (q >= a0) o[(long long)q * st] = v + cr[q];
+        if (qq >= a0) o[(long long)qq * st] = v + cr[qq];
 #pragma unroll
         for (int u = 0; u < 5; u++) w[u] = w[u + 1];
         w[5] = v;
 #pragma unroll
         for (int u = 6; u < 12; u++) w[u] = w[u + 1];
-        w[12] = (q + 7 < n) ? s[(long long)(q + 7) * st] : T(0);
+        w[12] = next;
+    };
+    // blocks of 8 steps, the next block's inputs loaded before this one runs
+    T nx[8];
+#pragma unroll
+    for (int t = 0; t < 8; t++) nx[t] = (q + 7 + t < n) ? s[(long long)(q + 7 + t) * st] : T(0);
+    for (; q + 8 <= b0; q += 8) {
+        T cur[8];
+#pragma unroll
+        for (int t = 0; t < 8; t++) {
+            cur[t] = nx[t];
+            nx[t] = (q + 15 + t < n) ? s[(long long)(q + 15 + t) * st] : T(0);
+        }
+#pragma unroll
+        for (int t = 0; t < 8; t++) step(q + t, cur[t]);
     }
+    for (; q < b0; q++) step(q, (q + 7 < n) ? s[(long long)(q + 7) * st] : T(0));
     if (c == chunks - 1) {
 #pragma unroll
         for (int x = 10; x >= 5; x--) w[x] = passb<T, -1>(w, x, fc.bm1, fc.b, fc.bsum);
@@ -554,6 +570,21 @@ __device__ void bc_item(const Args &a, int inst, T *qall)
     }
 }
 
+// Items handed out one per warp from a counter, largest first (the host
+// sorts the lists by cost): the phase ends close to total work / warps
+// instead of at the unluckiest warp's share.
+template <typename F>
+__device__ __forceinline__ void for_items(unsigned *ctr, int n, F &&f)
+{
+    for (;;) {
+        unsigned w = 0;
+        if ((threadIdx.x & 31) == 0) w = atomicAdd(ctr, 1u);
+        w = __shfl_sync(0xffffffffu, w, 0);
+        if ((int)w >= n) break;
+        f((int)w);
+    }
+}
+
 template <typename T, int TY>
 __global__ void __launch_bounds__(256) k_batch_step(Args a)
 {
@@ -570,9 +601,10 @@ __global__ void __launch_bounds__(256) k_batch_step(Args a)
         for (int it = blockIdx.x; it < a.ntiles; it += gridDim.x)
             stage_tile<T, TY>(a, st, a.tiles[it], qa, qb, smem);
         if (!grid_barrier(a)) return;
-        for (long long wi = gw; wi < a.nfx; wi += nwarps) fx_item<T, PW>(a, a.fx[wi], qb, qa, ti, to);
+        for_items(a.work + 2 * st, a.nfx,
+                  [&](int wi) { fx_item<T, PW>(a, a.fx[wi], qb, qa, ti, to); });
         if (!grid_barrier(a)) return;
-        for (long long wi = gw; wi < a.nfy; wi += nwarps) fy_item<T>(a, a.fy[wi], qa, qb);
+        for_items(a.work + 2 * st + 1, a.nfy, [&](int wi) { fy_item<T>(a, a.fy[wi], qa, qb); });
         if (!grid_barrier(a)) return;
         for (long long wi = gw; wi < a.nbc; wi += nwarps) bc_item<T>(a, a.bc[wi], qb);
         if (st < 5 && !grid_barrier(a)) return;
@@ -839,6 +871,9 @@ cudaError_t launch_step_t(ns_batch *b, cudaStream_t s)
 
 cudaError_t launch_step(ns_batch *b, cudaStream_t s)
 {
+    // the per-stage item counters start every step at zero
+    cudaError_t me = cudaMemsetAsync(b->bar + 2, 0, 12 * sizeof(unsigned), s);
+    if (me != cudaSuccess) return me;
     if (b->has_src) {
         ns::batch::k_batch_sin<<<1, 256, 0, s>>>(b->wf, b->dtv, b->n, b->d_iter, b->stage_sin);
         cudaError_t e = cudaGetLastError();
@@ -1094,6 +1129,19 @@ int ns_batch_create(const ns_params *const *params, int n, int precision, ns_bat
         }
         bcl.push_back(q);
     }
+    // filter items largest first: a chunk after the first also runs the warm-up
+    auto item_cost = [&](const int4 &it, bool along_x) {
+        const auto &in = hin[it.x];
+        const int n = along_x ? in.imax : in.jmax;
+        const int chunks = along_x ? in.fx_chunks : in.fy_chunks;
+        return (n - 12) / chunks + (it.w > 0 && in.warm > 0 ? in.warm : 0);
+    };
+    std::stable_sort(fxl.begin(), fxl.end(), [&](const int4 &p, const int4 &q) {
+        return item_cost(p, true) > item_cost(q, true);
+    });
+    std::stable_sort(fyl.begin(), fyl.end(), [&](const int4 &p, const int4 &q) {
+        return item_cost(p, false) > item_cost(q, false);
+    });
     b->ntiles[0] = (int)tiles8.size();
     b->ntiles[1] = (int)tiles16.size();
     b->nfx = (int)fxl.size();
@@ -1135,7 +1183,7 @@ int ns_batch_create(const ns_params *const *params, int n, int precision, ns_bat
     B_TRY(tput(b, &b->mdu, mdu, es));
     B_TRY(tput(b, &b->corr, corr, es));
     B_TRY(balloc(b, (unsigned char **)&b->src, std::max<long long>(soff, 1) * es));
-    B_TRY(balloc(b, &b->bar, 2));
+    B_TRY(balloc(b, &b->bar, 2 + 12));
     B_TRY(balloc(b, &b->err, 1));
     B_TRY(balloc(b, &b->d_iter, 1));
     if (cudaMemsetAsync(b->q[0], 0, b->qsize * es, b->stream) != cudaSuccess ||
@@ -1237,6 +1285,7 @@ int ns_batch_create(const ns_params *const *params, int n, int precision, ns_bat
         }
         a.bar_count = b->bar;
         a.bar_gen = b->bar + 1;
+        a.work = b->bar + 2;
         a.err = b->err;
         a.spin_limit = 20000000;  // x 64 ns sleeps: about 1-2 s per barrier
     }

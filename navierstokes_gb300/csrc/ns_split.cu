@@ -139,7 +139,7 @@ __device__ __forceinline__ void pair_scale(float &h, float &l, float s)
 }
 
 template <int NP, bool FIRST, bool SRC>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 4)
     k_split_stage(Dims d, int fpitch, const float *__restrict__ qin, float *__restrict__ qout,
                   double *__restrict__ W, const float *__restrict__ xc,
                   const float *__restrict__ yc, const float *__restrict__ xcl,
