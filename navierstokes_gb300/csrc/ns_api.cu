@@ -824,10 +824,34 @@ int ns_rk_euler(ns_ctx *c, double *U, double t, int iter, int nk)
     (void)t;
     if (!c || !U) return set_err(c, NS_ERR_PARAM, "ns_rk_euler: NULL argument");
     if (nk != c->d.nk) return set_err(c, NS_ERR_PARAM, "nk=%d, context has %d", nk, c->d.nk);
-    int rc = ns_set_state(c, U, NS_LAYOUT_FORTRAN);
-    if (rc == NS_OK) rc = ns_step(c, iter, 1);
-    if (rc == NS_OK) rc = ns_get_state(c, U, NS_LAYOUT_FORTRAN);
-    return rc;
+    NS_CUDA(c, cudaSetDevice(c->dev));
+    // Page-locked host memory that the device can address (every pinned
+    // allocation under unified addressing): the layout kernels read U from
+    // the host and write it back directly, one pass each way, with no
+    // staging copy.  Any other host memory goes through set/get state.
+    cudaPointerAttributes at{};
+    void *dev_view = nullptr;
+    if (cudaPointerGetAttributes(&at, U) == cudaSuccess && at.type == cudaMemoryTypeHost &&
+        at.devicePointer)
+        dev_view = at.devicePointer;
+    else
+        cudaGetLastError();
+    if (!dev_view) {
+        int rc = ns_set_state(c, U, NS_LAYOUT_FORTRAN);
+        if (rc == NS_OK) rc = ns_step(c, iter, 1);
+        if (rc == NS_OK) rc = ns_get_state(c, U, NS_LAYOUT_FORTRAN);
+        return rc;
+    }
+    double *hv = static_cast<double *>(dev_view);
+    NS_CUDA(c, ns::launch_aos_to_soa(hv, c->U, c->d, c->stream));
+    if (c->split) NS_CUDA(c, ns::launch_split_from_full(c, c->U, c->stream));
+    c->have_state = true;
+    const int rc = ns_step(c, iter, 1);
+    if (rc != NS_OK) return rc;
+    if (c->split) NS_CUDA(c, ns::launch_split_to_full(c, c->U, c->stream));
+    NS_CUDA(c, ns::launch_soa_to_aos(c->U, hv, c->d, c->stream));
+    NS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return NS_OK;
 }
 
 int ns_get_probes(ns_ctx *c, int np, const int32_t *pi, const int32_t *pj, double *out)

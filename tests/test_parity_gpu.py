@@ -128,6 +128,31 @@ def test_rk_euler_dropin_matches_resident(oracle_mod, nslib):
     assert_parity(U, ref, c.Ub, label="rk_euler drop-in")
 
 
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+def test_rk_euler_pinned_host_reads_directly(nslib, precision):
+    """ns_rk_euler on page-locked host memory: the layout kernels read and
+    write the host array in place; results equal the pageable path's."""
+    import torch
+    from navierstokes_gb300 import Solver
+    from navierstokes_gb300 import _lib as L
+    if precision == "fp64":
+        c, prec = cases.mixing_layer_case(imax=64, jmax=48, D=10), L.NS_PREC_FP64
+    else:
+        c, prec = cases.uniform_flow_case(imax=96, jmax=80, D=10, vortex_upstream=20), \
+            L.NS_PREC_SPLIT
+    pinned = torch.empty(c.U0.shape, dtype=torch.float64, pin_memory=True).numpy()
+    pinned[...] = c.U0
+    paged = c.U0.copy()
+    with Solver(c, precision=prec) as s:
+        for it in range(4):
+            s.rk_euler(pinned, (it + 1) * c.dt, it)
+    with Solver(c, precision=prec) as s:
+        for it in range(4):
+            s.rk_euler(paged, (it + 1) * c.dt, it)
+    assert np.array_equal(pinned, paged)
+    assert not np.array_equal(pinned, c.U0)
+
+
 def test_probes_and_layouts(nslib):
     from navierstokes_gb300 import Solver
     c = cases.acoustic_pulse_case(imax=50, jmax=40, D=8)
