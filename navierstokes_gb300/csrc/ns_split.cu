@@ -199,8 +199,8 @@ __global__ void __launch_bounds__(256, 4)
         float q[NPL], gx[NPL], gy[NPL];
         const float *cyp = yc + kCoefStride * j;
         const bool yint = (j >= 3 && j < d.jmax - 3);
-#pragma unroll
         const float *cylp = ycl + kCoefStride * j;
+#pragma unroll
         for (int k = 0; k < NPL; k++) {
             q[k] = sq[k][sr][sc];
             if (xint) {
@@ -635,9 +635,9 @@ __device__ __forceinline__ void filter_x_rows(const float *__restrict__ sbase,
 }
 
 template <int NP>
-__global__ void __launch_bounds__(32 * x_warps<NP>())
-    k_split_filter_x(Dims d, int fpitch, const float *__restrict__ src, float *__restrict__ dst,
-                     int chunks, int warm, FiltF f)
+__device__ __forceinline__ void split_filter_x_body(Dims d, int fpitch, const float *__restrict__ src,
+                                                    float *__restrict__ dst, int chunks, int warm,
+                                                    const FiltF &f)
 {
     constexpr int kXW = x_warps<NP>();
     constexpr int kXL = NP ? kXW : 1;  // lo tiles only when pairs exist
@@ -670,6 +670,22 @@ __global__ void __launch_bounds__(32 * x_warps<NP>())
         filter_x_rows<false>(src + k * fplane + roff, nullptr, dst + k * fplane + roff, nullptr,
                              fpitch, n, nrows, lane, a, b, exact, c == 0, c == chunks - 1, q0, f,
                              tin[wid], tout[wid], tinl[0], toutl[0]);
+}
+
+// Register budgets measured best: the all-FP32 variant at one block per SM
+// minimum (96 registers), the pair variant left to the compiler (111).
+__global__ void __launch_bounds__(32 * x_warps<0>(), 1)
+    k_split_filter_x_single(Dims d, int fpitch, const float *__restrict__ src,
+                            float *__restrict__ dst, int chunks, int warm, FiltF f)
+{
+    split_filter_x_body<0>(d, fpitch, src, dst, chunks, warm, f);
+}
+
+__global__ void __launch_bounds__(32 * x_warps<3>())
+    k_split_filter_x_pairs(Dims d, int fpitch, const float *__restrict__ src,
+                           float *__restrict__ dst, int chunks, int warm, FiltF f)
+{
+    split_filter_x_body<3>(d, fpitch, src, dst, chunks, warm, f);
 }
 
 // ---------------------------------------------------------------------------
@@ -823,8 +839,13 @@ static cudaError_t launch_split_np(ns_ctx *c, int cls, int stage, cudaStream_t s
     case NS_KC_SPLIT_FX: {
         const long long warps = (long long)((d.jmax + 31) / 32) * 4 * sp.fx_chunks;
         constexpr int kXW = x_warps<NP>();
-        k_split_filter_x<NP><<<(unsigned)((warps + kXW - 1) / kXW), 32 * kXW, 0, s>>>(
-            d, sp.fpitch, qb, qa, sp.fx_chunks, sp.warm, to_f32(c->fx));
+        const unsigned nb = (unsigned)((warps + kXW - 1) / kXW);
+        if (NP)
+            k_split_filter_x_pairs<<<nb, 32 * kXW, 0, s>>>(d, sp.fpitch, qb, qa, sp.fx_chunks,
+                                                           sp.warm, to_f32(c->fx));
+        else
+            k_split_filter_x_single<<<nb, 32 * kXW, 0, s>>>(d, sp.fpitch, qb, qa, sp.fx_chunks,
+                                                            sp.warm, to_f32(c->fx));
         break;
     }
     case NS_KC_SPLIT_FY: {
