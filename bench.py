@@ -231,7 +231,7 @@ SPLIT32_BYTES_PER_POINT = {"k_split_stage": 96, "k_split_filter_x": 32,
 
 
 def split_study(args, local, hbm_peak):
-    """Config-3 workload: Euler, 4096x4096 uniform grid, M = 0.5, pulse 1e-4,
+    """The split-precision workload: Euler, 4096x4096 uniform grid, M = 0.5, pulse 1e-4,
     vortex 1e-3, 1000 steps; split precision (u', v', p' as FP32 pairs) and
     the all-FP32 split against plain FP64 (throughput of each and p' = p - p_b
     error at steps 100/500/1000)."""
@@ -330,7 +330,7 @@ def split_study(args, local, hbm_peak):
 
 
 def batch_study(args, local):
-    """Config-4 workload: 64 independent Euler instances, sizes log-uniform in
+    """The parameter-sweep workload: 64 independent Euler instances, sizes log-uniform in
     [128, 1024] (multiples of 32), monopole sources, mean flow M ~ U[0, 0.6],
     numpy.random.default_rng(0); 300 steps in one persistent launch per step,
     FP64 and split precision, tiles autotuned."""
@@ -379,7 +379,7 @@ def batch_study(args, local):
 
 
 def adjoint_study(args, local):
-    """Config-5 workload: Euler on 512x512 with M = 0.3, a Gaussian monopole
+    """The adjoint workload: Euler on 512x512 with M = 0.3, a Gaussian monopole
     source field (b = 32 cells) whose amplitude is the Keys-cubic
     interpolant of 16x16 controls ~ N(0, 1e-3) (seed 0), omega = 0.5, 2000
     steps; loss = sum over steps of p'^2 at 32 observers on a circle of
@@ -458,21 +458,21 @@ def cpu_baseline_sample(case, seconds=20.0):
                       f"untimed step, C oracle (-O3, OpenMP over lines)"}
 
 
-def cpu_configs_study(seconds=8.0):
-    """The C oracle on every configuration's workload, on all host cores and
-    on one core: a bounded sample of steps each (the per-step rate is what
-    is reported).  Configuration 4 times its 64 instances one after the
-    other; configuration 5 times the forward step of the source problem."""
+def cpu_workloads_study(seconds=8.0):
+    """The C oracle on every workload of this benchmark, on all host cores
+    and on one core: a bounded sample of steps each (the per-step rate is
+    what is reported).  The sweep times its 64 instances one after the
+    other; the source problem times its forward step."""
     import oracle
     from navierstokes_gb300 import cases
     from navierstokes_gb300.adjoint import SourceProblem
     oracle.build()
     allc = os.cpu_count() or 1
-    work = [("1: 201x201 Euler pulse", [cases.acoustic_pulse_case()]),
-            ("2: 4096x2048 Navier-Stokes", [cases.stretched_ns_case()]),
-            ("3: 4096x4096 Euler, pulse + vortex", [cases.uniform_flow_case()]),
-            ("4: 64 Euler instances (seed 0)", cases.sweep_cases(n=64, seed=0)),
-            ("5: 512x512 Euler with source field", [SourceProblem(steps=10).case])]
+    work = [("201x201 Euler pulse", [cases.acoustic_pulse_case()]),
+            ("4096x2048 Navier-Stokes", [cases.stretched_ns_case()]),
+            ("4096x4096 Euler, pulse + vortex", [cases.uniform_flow_case()]),
+            ("64 Euler instances (seed 0)", cases.sweep_cases(n=64, seed=0)),
+            ("512x512 Euler with source field", [SourceProblem(steps=10).case])]
     out = {}
     for name, cs in work:
         row = {}
@@ -502,7 +502,7 @@ def cpu_configs_study(seconds=8.0):
     oracle.set_threads(allc)
     return {"unit": UNIT, "cores": allc, "kind": "port",
             "sample": "C oracle (-O3, OpenMP over lines), a few steps of each workload",
-            "configs": out}
+            "workloads": out}
 
 
 def run_ours(args, world, rank, local, pg):
@@ -629,12 +629,12 @@ def run_ours(args, world, rank, local, pg):
         except Exception as e:
             adjoint = {"failed": str(e)}
 
-    cpu_configs = None
-    if rank == 0 and world == 1 and args.cpu_configs:
+    cpu_workloads = None
+    if rank == 0 and world == 1 and args.cpu_workloads:
         try:
-            cpu_configs = cpu_configs_study()
+            cpu_workloads = cpu_workloads_study()
         except Exception as e:
-            cpu_configs = {"failed": str(e)}
+            cpu_workloads = {"failed": str(e)}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -665,8 +665,8 @@ def run_ours(args, world, rank, local, pg):
             line["batched"] = batched
         if adjoint is not None:
             line["adjoint"] = adjoint
-        if cpu_configs is not None:
-            line["cpu_configs"] = cpu_configs
+        if cpu_workloads is not None:
+            line["cpu_workloads"] = cpu_workloads
         print(json.dumps(line), flush=True)
 
 
@@ -681,16 +681,16 @@ def main():
     ap.add_argument("--nk", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-split", action="store_true",
-                    help="skip the split-precision (config-3) study")
+                    help="skip the split-precision study (Euler 4096^2)")
     ap.add_argument("--split-n", type=int, default=4096)
     ap.add_argument("--no-batch", action="store_true",
-                    help="skip the batched-sweep (config-4) study")
+                    help="skip the batched-sweep study (64 instances)")
     ap.add_argument("--batch-n", type=int, default=64)
     ap.add_argument("--batch-steps", type=int, default=300)
     ap.add_argument("--no-adjoint", action="store_true",
-                    help="skip the discrete-adjoint (config-5) study")
-    ap.add_argument("--cpu-configs", action="store_true",
-                    help="also time the C oracle on every configuration (all cores, 1 core)")
+                    help="skip the discrete-adjoint study (512^2, 2000 steps)")
+    ap.add_argument("--cpu-workloads", action="store_true",
+                    help="also time the C oracle on every workload (all cores, 1 core)")
     ap.add_argument("--adjoint-steps", type=int, default=2000)
     ap.add_argument("--adjoint-k", type=int, default=100)
     ap.add_argument("--split-error-steps", type=lambda t: [int(x) for x in t.split(",")],

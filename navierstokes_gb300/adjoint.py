@@ -47,7 +47,7 @@ def cubic_basis(n: int, nc: int) -> np.ndarray:
 
 
 class SourceProblem:
-    """Config-5 problem: the case, the control basis and the observers."""
+    """The source problem: the case, the control basis and the observers."""
 
     def __init__(self, n=512, nc=16, mach=0.3, omega=0.5, steps=2000, radius=150.0, nobs=32,
                  envelope_cells=32.0, D=30, sigmaf=0.2, seed=0, control_std=1e-3):

@@ -42,12 +42,12 @@ def test_acoustic_pulse_short(oracle_mod, nslib, nk):
     assert_parity(got, ref, c.Ub, label=f"pulse nk={nk}")
 
 
-def test_acoustic_pulse_config1_full(oracle_mod, nslib):
+def test_acoustic_pulse_201x201_500_steps(oracle_mod, nslib):
     """201x201 Euler pulse, sigma_f = 0.2, D = 30, CFL 0.5, 500 steps."""
     c = cases.acoustic_pulse_case()
     got, ref = _run_both(oracle_mod, c, 500)
-    errs = assert_parity(got, ref, c.Ub, label="config-1 pulse 201x201x500")
-    print("config-1 per-variable (rel max, rel perturbation):", errs)
+    errs = assert_parity(got, ref, c.Ub, label="pulse 201x201, 500 steps")
+    print("pulse 201x201 per variable (rel max, rel perturbation):", errs)
 
 
 def test_mixing_layer_reference_case(oracle_mod, nslib):
@@ -105,11 +105,11 @@ def test_uniform_state_is_fixed_point(oracle_mod, nslib):
     assert_parity(U, ref, c.Ub, label="uniform state 4096x2048")
 
 
-def test_full_size_config2_two_steps(oracle_mod, nslib):
+def test_navier_stokes_4096x2048_two_steps(oracle_mod, nslib):
     """4096x2048 Navier-Stokes, two steps, GPU vs oracle at full size."""
     c = cases.stretched_ns_case()
     got, ref = _run_both(oracle_mod, c, 2)
-    assert_parity(got, ref, c.Ub, label="config-2 full size, 2 steps")
+    assert_parity(got, ref, c.Ub, label="Navier-Stokes 4096x2048, 2 steps")
 
 
 def test_rk_euler_dropin_matches_resident(oracle_mod, nslib):
