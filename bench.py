@@ -53,7 +53,7 @@ FP64_INST_PER_POINT = {"k_prim": 7.0, "k_first": 112.03, "k_update": 74.82,
 # (2048x2048), scaled to a launch by the number of points.
 TRAFFIC_PER_POINT = {"k_prim": 21.3, "k_first": 130.4, "k_update": 230.6,
                      "k_filter_x": 61.8, "k_filter_y": 61.8}
-FP64_PEAK_FALLBACK_TFLOPS = 1.19  # DFMA throughput measured on the GB300s
+FP64_PEAK_FALLBACK_TFLOPS = 1.19  # DFMA throughput measured on GB300 (profiles/fp64_peak.md)
 STEP_BYTES_FUSED_MIN = 1536  # compulsory bytes per point-step of a fused FP64 design, nk = 4
 
 

@@ -43,7 +43,7 @@ typedef enum ns_status {
     NS_ERR_NONFINITE = 4,   /* the state holds NaN/Inf (ns_check_finite) */
     NS_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up */
     NS_ERR_STATE = 6,       /* call out of order (e.g. step before set_state) */
-    NS_ERR_UNSUPPORTED = 7  /* feature not available in this build/context */
+    NS_ERR_UNSUPPORTED = 7  /* feature not available for these parameters */
 } ns_status;
 
 /* Host array layouts accepted by ns_set_state/ns_get_state. */

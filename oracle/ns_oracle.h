@@ -3,7 +3,7 @@
  * mathe1s/NavierStokes (rk.f90 and everything it calls).
  *
  * TEST INFRASTRUCTURE ONLY.  This is a plain-C, FP64, line-by-line
- * restatement of the Fortran reference.  It is the checker for the CUDA
+ * restatement of the Fortran reference.  It is the reference for the CUDA
  * path (tests/, __graft_entry__.smoke(), bench.py's CPU baseline) and is
  * never linked into, loaded by, or called from the product library.
  *
