@@ -3,8 +3,8 @@
  * mathe1s/NavierStokes (rk.f90 and everything it calls).
  *
  * TEST INFRASTRUCTURE ONLY.  This is a plain-C, FP64, line-by-line
- * restatement of the Fortran reference.  It is the reference for the CUDA
- * path (tests/, __graft_entry__.smoke(), bench.py's CPU baseline) and is
+ * restatement of the Fortran reference.  The CUDA path is checked against
+ * it (tests/, __graft_entry__.smoke(), bench.py's CPU baseline); it is
  * never linked into, loaded by, or called from the product library.
  *
  * Parity status: the reference ships no tests, fixtures or golden vectors
