@@ -62,6 +62,39 @@ __device__ __forceinline__ float d2f_rn(double x)
     return __uint_as_float(f);
 }
 
+// hi = x rounded to FP32 (nearest even) and lo = x - hi rounded to FP32, with
+// integer operations and one integer-to-float conversion, no FP64-pipe
+// instruction: the remainder is the 29 discarded mantissa bits, minus 2^29
+// when hi rounded up, times 2^(e - 1075).  Zero, |x| < 2^-74 and |x| >= 2^128
+// take the plain conversions.
+__device__ __forceinline__ void d2f_split(double x, float &hi, float &lo)
+{
+    const unsigned xh = (unsigned)__double2hiint(x), xl = (unsigned)__double2loint(x);
+    const unsigned e = (xh >> 20) & 0x7ffu;
+    if (((xh & 0x7fffffffu) | xl) == 0u) {
+        hi = __uint_as_float(xh & 0x80000000u);
+        lo = 0.f;
+        return;
+    }
+    if (e < 949u || e > 1150u) {
+        hi = d2f_rn(x);
+        lo = d2f_rn(x - f2d_exact(hi));
+        return;
+    }
+    const unsigned top = ((xh & 0xfffffu) << 3) | (xl >> 29);  // 23 mantissa bits
+    const unsigned rest = xl & 0x1fffffffu;                    // 29 discarded bits
+    unsigned f = (xh & 0x80000000u) | ((e - 896u) << 23) | top;
+    int r = (int)rest;
+    const unsigned half = 1u << 28;
+    if (rest > half || (rest == half && (top & 1u))) {  // carry may bump the exponent
+        f += 1u;
+        r -= (1 << 29);
+    }
+    hi = __uint_as_float(f);
+    const float mag = __int2float_rn(r) * __uint_as_float((e - 948u) << 23);
+    lo = (xh & 0x80000000u) ? -mag : mag;
+}
+
 // ---------------------------------------------------------------------------
 // Fused stage kernel: FP32 derivatives from a shared-memory tile, Euler RHS,
 // FP64 LDDRK update, buffer damping.  Out of place (qin -> qout).
@@ -296,10 +329,12 @@ __global__ void __launch_bounds__(256, 4)
                 const double w = FIRST ? dr : fma(alpha, wold[h][k], dr);
                 W[k * d.plane + didx] = w;
                 if (is_pair<NP>(k)) {
+                    // hi + beta*w in FP64, split exactly; the old lo joins in FP32
+                    // (both parts are below an FP32 ulp of hi)
                     float &lo = q[is_pair<NP>(k) ? k + 3 : k];
-                    const double v = fma(beta, w, f2d_exact(q[k]) + f2d_exact(lo));
-                    const float hi = d2f_rn(v);
-                    lo = d2f_rn(v - f2d_exact(hi));
+                    float hi, rem;
+                    d2f_split(fma(beta, w, f2d_exact(q[k])), hi, rem);
+                    lo = rem + lo;
                     q[k] = hi;
                 } else {
                     q[k] = d2f_rn(fma(beta, w, f2d_exact(q[k])));
