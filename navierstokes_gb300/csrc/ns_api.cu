@@ -13,6 +13,9 @@
 #include <cstring>
 #include <vector>
 
+#include <cudaTypedefs.h>
+#include <mutex>
+
 #include "ns_internal.cuh"
 
 #define NS_STR2(x) #x
@@ -280,6 +283,7 @@ void free_all(ns_ctx *c)
                        sp.rho_bc, sp.ycorr, sp.mean_buf};
         for (float *b : fb)
             if (b) cudaFree(b);
+        if (sp.err) cudaFree(sp.err);
     }
     if (c->step_exec) cudaGraphExecDestroy(c->step_exec);
     double *bufs[] = {c->U,    c->U2,   c->W,     c->dudm, c->dudn, c->aux,
@@ -364,6 +368,45 @@ int upload_field(ns_ctx *c, const double *h, int layout, double *dplanes)
     return NS_OK;
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library).
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                             &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        else
+            cudaGetLastError();
+    });
+    return fn;
+}
+
+// TMA map of one perturbation buffer: planes of jmax rows of fpitch floats;
+// box 40 x 22 x planes (the stage kernel's halo tile)
+int make_split_map(ns_ctx *c, CUtensorMap *map, float *base, int planes)
+{
+    const auto encode = tensor_map_encoder();
+    if (!encode) return set_err(c, NS_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled is unavailable");
+    const ns::Dims &d = c->d;
+    const cuuint64_t dims[3] = {(cuuint64_t)d.imax, (cuuint64_t)d.jmax, (cuuint64_t)planes};
+    const cuuint64_t strides[2] = {(cuuint64_t)c->sp.fpitch * sizeof(float),
+                                   (cuuint64_t)c->sp.fpitch * d.jmax * sizeof(float)};
+    const cuuint32_t box[3] = {40u, 22u, (cuuint32_t)planes};
+    const cuuint32_t estr[3] = {1u, 1u, 1u};
+    const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box,
+                              estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_err(c, NS_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return NS_OK;
+}
+
 // Split precision: FP64 base flow + FP32 perturbation (ns_split.cu).
 int create_split(ns_ctx *c)
 {
@@ -405,15 +448,19 @@ int create_split(ns_ctx *c)
         (rc = dalloc(c, &sp.rho_bc, (size_t)jmax)) || (rc = dalloc(c, &sp.ycorr, 4 * (size_t)jmax)) ||
         (rc = dalloc(c, &sp.mean_buf, 4 * (size_t)jmax)) ||
         (rc = dalloc(c, &c->stage_sin, 8)) || (rc = dalloc(c, &c->d_iter, 1)) ||
-        (rc = dalloc(c, &c->d_count, 1)))
+        (rc = dalloc(c, &c->d_count, 1)) || (rc = dalloc(c, &sp.err, 1)))
         return rc;
     if (p->source_mode != NS_SRC_NONE && (rc = dalloc(c, &sp.src, FP))) return rc;
+    if ((rc = make_split_map(c, &sp.qmap[0], sp.q[0], 4 + sp.np)) ||
+        (rc = make_split_map(c, &sp.qmap[1], sp.q[1], 4 + sp.np)))
+        return rc;
     cudaError_t e = cudaMemsetAsync(sp.q[0], 0, (4 + sp.np) * FP * sizeof(float), c->stream);
     if (e == cudaSuccess)
         e = cudaMemsetAsync(sp.q[1], 0, (4 + sp.np) * FP * sizeof(float), c->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->W, 0, nk * P * sizeof(double), c->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->d_iter, 0, sizeof(int), c->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->stage_sin, 0, 8 * sizeof(double), c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(sp.err, 0, sizeof(int), c->stream);
     if (e != cudaSuccess) return cuda_err(c, e, "cudaMemset");
 
     std::vector<double> tx, ty;
@@ -752,6 +799,8 @@ int ns_set_state(ns_ctx *c, const double *U, int layout)
     return NS_OK;
 }
 
+static int check_split_err(ns_ctx *c);
+
 int ns_get_state(ns_ctx *c, double *U, int layout)
 {
     if (!c || !U) return set_err(c, NS_ERR_PARAM, "ns_get_state: NULL argument");
@@ -771,7 +820,7 @@ int ns_get_state(ns_ctx *c, double *U, int layout)
         return set_err(c, NS_ERR_PARAM, "layout=%d", layout);
     }
     NS_CUDA(c, cudaStreamSynchronize(c->stream));
-    return NS_OK;
+    return check_split_err(c);
 }
 
 static int ensure_graph(ns_ctx *c)
@@ -811,12 +860,26 @@ int ns_step(ns_ctx *c, int iter0, int nsteps)
     return NS_OK;
 }
 
+// A split-precision stage kernel whose TMA wait gave up leaves its error word
+// set; it is reported (and cleared) at the next synchronisation.
+static int check_split_err(ns_ctx *c)
+{
+    if (!c->split || !c->sp.err) return NS_OK;
+    int h = 0;
+    NS_CUDA(c, cudaMemcpyAsync(&h, c->sp.err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    NS_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (!h) return NS_OK;
+    NS_CUDA(c, cudaMemsetAsync(c->sp.err, 0, sizeof(int), c->stream));
+    NS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return set_err(c, NS_ERR_TIMEOUT, "a split-precision stage kernel timed out waiting for its TMA tile");
+}
+
 int ns_synchronize(ns_ctx *c)
 {
     if (!c) return set_err(nullptr, NS_ERR_PARAM, "ns_synchronize: NULL context");
     NS_CUDA(c, cudaSetDevice(c->dev));
     NS_CUDA(c, cudaStreamSynchronize(c->stream));
-    return NS_OK;
+    return check_split_err(c);
 }
 
 int ns_rk_euler(ns_ctx *c, double *U, double t, int iter, int nk)
@@ -851,7 +914,7 @@ int ns_rk_euler(ns_ctx *c, double *U, double t, int iter, int nk)
     if (c->split) NS_CUDA(c, ns::launch_split_to_full(c, c->U, c->stream));
     NS_CUDA(c, ns::launch_soa_to_aos(c->U, hv, c->d, c->stream));
     NS_CUDA(c, cudaStreamSynchronize(c->stream));
-    return NS_OK;
+    return check_split_err(c);
 }
 
 int ns_get_probes(ns_ctx *c, int np, const int32_t *pi, const int32_t *pj, double *out)

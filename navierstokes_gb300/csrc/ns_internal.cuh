@@ -7,6 +7,7 @@
 // j*pitch + i.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string>
@@ -108,6 +109,8 @@ struct SplitState {
     // p', then the lo parts
     int np = 3;
     float *q[2] = {nullptr, nullptr}; // perturbation ping-pong
+    CUtensorMap qmap[2];              // TMA maps of q[0], q[1]: (imax, jmax, 4 + np) FP32
+    int *err = nullptr;               // set by a stage kernel whose TMA wait gave up
     float *xc = nullptr, *yc = nullptr;
     float *xcl = nullptr, *ycl = nullptr;  // FP64 table minus its FP32 rounding
     float *sigx = nullptr, *sigy = nullptr, *src = nullptr;

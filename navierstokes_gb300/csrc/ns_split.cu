@@ -100,7 +100,62 @@ __device__ __forceinline__ void d2f_split(double x, float &hi, float &lo)
 // FP64 LDDRK update, buffer damping.  Out of place (qin -> qout).
 // ---------------------------------------------------------------------------
 constexpr int kTX = 32, kTY = 16, kH = 3;
-constexpr int kSW = kTX + 2 * kH, kSH = kTY + 2 * kH;
+constexpr int kSH = kTY + 2 * kH;
+// Tile width in shared memory: the TMA box starts 4 columns left of the
+// block (its x coordinate times 4 bytes must be a multiple of 16) and spans
+// 40 columns (a multiple of 16 bytes): i0-4 .. i0+35 covers the halo of 3.
+constexpr int kTL = 4, kSW = 40;
+
+// ---------------------------------------------------------------------------
+// TMA: one cp.async.bulk.tensor per block brings the whole halo tile of every
+// plane into shared memory; an mbarrier counts its bytes.  Every wait on the
+// barrier is bounded: a block that gives up sets the context's error word
+// and returns (the host reports NS_ERR_TIMEOUT).
+// ---------------------------------------------------------------------------
+constexpr long long kTmaSpinLimit = 1LL << 24;
+
+__device__ __forceinline__ unsigned smem_addr(const void *p)
+{
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+                 : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity)
+{
+    unsigned done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int x, int y, int z,
+                                            unsigned long long *bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_addr(dst)),
+        "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(z),
+        "r"(smem_addr(bar))
+        : "memory");
+}
 
 // One-sided closure, written as sum_z c_z*(f_z - f_q): the closure
 // coefficients sum to zero, and in this form a constant field gives exactly
@@ -173,7 +228,8 @@ __device__ __forceinline__ void pair_scale(float &h, float &l, float s)
 
 template <int NP, bool FIRST, bool SRC>
 __global__ void __launch_bounds__(256, 4)
-    k_split_stage(Dims d, int fpitch, const float *__restrict__ qin, float *__restrict__ qout,
+    k_split_stage(const __grid_constant__ CUtensorMap qmap, int *__restrict__ err, Dims d,
+                  int fpitch, const float *__restrict__ qin, float *__restrict__ qout,
                   double *__restrict__ W, const float *__restrict__ xc,
                   const float *__restrict__ yc, const float *__restrict__ xcl,
                   const float *__restrict__ ycl, const SplitMean mean,
@@ -182,10 +238,20 @@ __global__ void __launch_bounds__(256, 4)
                   float dt, double alpha, double beta, int stage)
 {
     constexpr int NPL = 4 + NP;
-    __shared__ float sq[NPL][kSH][kSW];
+    __shared__ alignas(128) float sq[NPL][kSH][kSW];
+    __shared__ alignas(8) unsigned long long tbar;
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int i0 = blockIdx.x * kTX, j0 = blockIdx.y * kTY;
     const long long fplane = (long long)fpitch * d.jmax;
+    const bool lead = (tx == 0 && ty == 0);
+    if (lead) mbar_init(&tbar, 1);
+    __syncthreads();
+    if (lead) {
+        // the box (40 x 22 x NPL floats) starts at (i0-4, j0-3, 0); points
+        // outside the grid read as zero and are never used
+        mbar_expect_tx(&tbar, (unsigned)sizeof(sq));
+        tma_load_3d(&sq[0][0][0], &qmap, i0 - kTL, j0 - kH, 0, &tbar);
+    }
     // the FP64 accumulators of this thread's two points, requested before
     // the tile so that their latency overlaps the tile load
     double wold[2][4];
@@ -199,19 +265,15 @@ __global__ void __launch_bounds__(256, 4)
             for (int k = 0; k < 4; k++) wold[h][k] = ok ? W[k * d.plane + didx] : 0.0;
         }
     }
-    // cooperative tile load (halo 3; points outside the grid are never read)
-    for (int r = ty; r < kSH; r += 8) {
-        const int gj = j0 - kH + r;
-        const bool rowok = gj >= 0 && gj < d.jmax;
-        for (int cc = tx; cc < kSW; cc += kTX) {
-            const int gi = i0 - kH + cc;
-            const bool ok = rowok && gi >= 0 && gi < d.imax;
-            const long long g = (long long)gj * fpitch + gi;
-#pragma unroll
-            for (int k = 0; k < NPL; k++) sq[k][r][cc] = ok ? qin[k * fplane + g] : 0.f;
+    {
+        long long spins = 0;
+        while (!mbar_try_wait(&tbar, 0)) {
+            if (++spins > kTmaSpinLimit) {
+                if (lead) atomicExch(err, 1);
+                return;
+            }
         }
     }
-    __syncthreads();
     const int i = i0 + tx;
     if (i >= d.imax) return;
     const float *cxp = xc + kCoefStride * i;
@@ -228,7 +290,7 @@ __global__ void __launch_bounds__(256, 4)
         if (j >= d.jmax) break;
         const long long fidx = (long long)j * fpitch + i;
         const long long didx = (long long)j * d.pitch + i;
-        const int sr = ly + kH, sc = tx + kH;
+        const int sr = ly + kH, sc = tx + kTL;
         float q[NPL], gx[NPL], gy[NPL];
         const float *cyp = yc + kCoefStride * j;
         const bool yint = (j >= 3 && j < d.jmax - 3);
@@ -861,8 +923,9 @@ static cudaError_t launch_split_np(ns_ctx *c, int cls, int stage, cudaStream_t s
         const bool src = sp.src != nullptr;
 #define NS_SPL(FIRST, SRC)                                                                      \
     k_split_stage<NP, FIRST, SRC><<<grd, blk, 0, s>>>(                                          \
-        d, sp.fpitch, qa, qb, c->W, sp.xc, sp.yc, sp.xcl, sp.ycl, sp.mean, sp.sigx, sp.sigy,    \
-        sp.src, c->stage_sin, (float)c->p.dt, c->alpha[stage], c->beta[stage], stage)
+        sp.qmap[stage & 1], sp.err, d, sp.fpitch, qa, qb, c->W, sp.xc, sp.yc, sp.xcl, sp.ycl,   \
+        sp.mean, sp.sigx, sp.sigy, sp.src, c->stage_sin, (float)c->p.dt, c->alpha[stage],        \
+        c->beta[stage], stage)
         if (stage == 0) {
             if (src) NS_SPL(true, true); else NS_SPL(true, false);
         } else {
