@@ -605,7 +605,7 @@ int ns_adjoint_forward(ns_adjoint *a, const double *U0, int layout, int iter0, i
     }
     A_CUDA(a, cudaMemcpyAsync(a->endstate, c->U, 4 * P * sizeof(double), cudaMemcpyDeviceToDevice, s));
     A_CUDA(a, cudaMemcpyAsync(loss, a->loss, sizeof(double), cudaMemcpyDeviceToHost, s));
-    A_CUDA(a, cudaStreamSynchronize(s));
+    if ((rc = ns_synchronize(c)) != NS_OK) return aerr(a, rc, ns_last_error(c));
     a->nsteps = nsteps;
     a->iter0 = iter0;
     a->forward_done = true;
@@ -648,7 +648,7 @@ int ns_adjoint_backward(ns_adjoint *a, double *grad_field)
     const size_t row = (size_t)d.imax * sizeof(double);
     A_CUDA(a, cudaMemcpy2DAsync(grad_field, row, a->gS, d.pitch * sizeof(double), row,
                                 (size_t)d.jmax, cudaMemcpyDeviceToHost, s));
-    A_CUDA(a, cudaStreamSynchronize(s));
+    if ((rc = ns_synchronize(c)) != NS_OK) return aerr(a, rc, ns_last_error(c));
     // leave the context's state at the forward end state
     A_CUDA(a, cudaMemcpy(c->U, a->endstate, 4 * P * sizeof(double), cudaMemcpyDeviceToDevice));
     return NS_OK;

@@ -283,7 +283,6 @@ void free_all(ns_ctx *c)
                        sp.rho_bc, sp.ycorr, sp.mean_buf};
         for (float *b : fb)
             if (b) cudaFree(b);
-        if (sp.err) cudaFree(sp.err);
     }
     if (c->step_exec) cudaGraphExecDestroy(c->step_exec);
     double *bufs[] = {c->U,    c->U2,   c->W,     c->dudm, c->dudn, c->aux,
@@ -294,6 +293,7 @@ void free_all(ns_ctx *c)
         if (b) cudaFree(b);
     if (c->d_iter) cudaFree(c->d_iter);
     if (c->d_count) cudaFree(c->d_count);
+    if (c->d_err) cudaFree(c->d_err);
     if (c->probe_idx) cudaFree(c->probe_idx);
     if (c->rec_idx) cudaFree(c->rec_idx);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
@@ -407,6 +407,41 @@ int make_split_map(ns_ctx *c, CUtensorMap *map, float *base, int planes)
     return NS_OK;
 }
 
+// TMA map of `depth` planes of pitch x jmax doubles from `base`, box
+// 40 x 14 x planes (the halo tile of the FP64 stage kernels); depth 0 means
+// depth = planes.
+static int make_fp64_map(ns_ctx *c, CUtensorMap *map, double *base, int planes,
+                         int depth = 0)
+{
+    if (depth == 0) depth = planes;
+    const auto encode = tensor_map_encoder();
+    if (!encode) return set_err(c, NS_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled is unavailable");
+    const ns::Dims &d = c->d;
+    const cuuint64_t dims[3] = {(cuuint64_t)d.imax, (cuuint64_t)d.jmax, (cuuint64_t)depth};
+    const cuuint64_t strides[2] = {(cuuint64_t)d.pitch * sizeof(double),
+                                   (cuuint64_t)d.plane * sizeof(double)};
+    const cuuint32_t box[3] = {(cuuint32_t)ns::kFirstTileW, (cuuint32_t)ns::kFirstTileH,
+                               (cuuint32_t)planes};
+    const cuuint32_t estr[3] = {1u, 1u, 1u};
+    const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, base, dims, strides, box,
+                              estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_err(c, NS_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return NS_OK;
+}
+
+static int make_fp64_maps(ns_ctx *c)
+{
+    // k_update's box: tau1..k dT/dy (viscous) and psiDiff (nk = 5)
+    const int nz = (c->visc ? 5 : 0) + (c->d.nk >= 5 ? 1 : 0);
+    int rc = make_fp64_map(c, &c->umap, c->U, c->d.nk);
+    if (rc == NS_OK) rc = make_fp64_map(c, &c->tmap, c->aux + (size_t)ns::AUX_T * c->d.plane, 1);
+    if (rc == NS_OK && nz > 0) rc = make_fp64_map(c, &c->amap, c->aux, nz, ns::AUX_COUNT);
+    c->fp64_maps = (rc == NS_OK);
+    return rc;
+}
+
 // Split precision: FP64 base flow + FP32 perturbation (ns_split.cu).
 int create_split(ns_ctx *c)
 {
@@ -448,7 +483,7 @@ int create_split(ns_ctx *c)
         (rc = dalloc(c, &sp.rho_bc, (size_t)jmax)) || (rc = dalloc(c, &sp.ycorr, 4 * (size_t)jmax)) ||
         (rc = dalloc(c, &sp.mean_buf, 4 * (size_t)jmax)) ||
         (rc = dalloc(c, &c->stage_sin, 8)) || (rc = dalloc(c, &c->d_iter, 1)) ||
-        (rc = dalloc(c, &c->d_count, 1)) || (rc = dalloc(c, &sp.err, 1)))
+        (rc = dalloc(c, &c->d_count, 1)) || (rc = dalloc(c, &c->d_err, 1)))
         return rc;
     if (p->source_mode != NS_SRC_NONE && (rc = dalloc(c, &sp.src, FP))) return rc;
     if ((rc = make_split_map(c, &sp.qmap[0], sp.q[0], 4 + sp.np)) ||
@@ -460,7 +495,7 @@ int create_split(ns_ctx *c)
     if (e == cudaSuccess) e = cudaMemsetAsync(c->W, 0, nk * P * sizeof(double), c->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->d_iter, 0, sizeof(int), c->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->stage_sin, 0, 8 * sizeof(double), c->stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(sp.err, 0, sizeof(int), c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
     if (e != cudaSuccess) return cuda_err(c, e, "cudaMemset");
 
     std::vector<double> tx, ty;
@@ -650,7 +685,9 @@ int ns_create(const ns_params *p, ns_ctx **out)
     NS_TRY(dalloc(c, &c->stage_sin, 8));
     NS_TRY(dalloc(c, &c->d_iter, 1));
     NS_TRY(dalloc(c, &c->d_count, 1));
+    NS_TRY(dalloc(c, &c->d_err, 1));
     if (p->source_mode != NS_SRC_NONE) NS_TRY(dalloc(c, &c->src, P));
+    NS_TRY(make_fp64_maps(c));
 
     {
         // zero everything so padding and never-written planes are defined
@@ -664,6 +701,8 @@ int ns_create(const ns_params *p, ns_ctx **out)
         e = cudaMemsetAsync(c->stage_sin, 0, 8 * sizeof(double), c->stream);
         if (e != cudaSuccess) { rc = cuda_err(c, e, "cudaMemset"); goto fail; }
         e = cudaMemsetAsync(c->d_iter, 0, sizeof(int), c->stream);
+        if (e != cudaSuccess) { rc = cuda_err(c, e, "cudaMemset"); goto fail; }
+        e = cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
         if (e != cudaSuccess) { rc = cuda_err(c, e, "cudaMemset"); goto fail; }
     }
 
@@ -799,7 +838,7 @@ int ns_set_state(ns_ctx *c, const double *U, int layout)
     return NS_OK;
 }
 
-static int check_split_err(ns_ctx *c);
+static int check_kernel_err(ns_ctx *c);
 
 int ns_get_state(ns_ctx *c, double *U, int layout)
 {
@@ -820,7 +859,7 @@ int ns_get_state(ns_ctx *c, double *U, int layout)
         return set_err(c, NS_ERR_PARAM, "layout=%d", layout);
     }
     NS_CUDA(c, cudaStreamSynchronize(c->stream));
-    return check_split_err(c);
+    return check_kernel_err(c);
 }
 
 static int ensure_graph(ns_ctx *c)
@@ -860,18 +899,18 @@ int ns_step(ns_ctx *c, int iter0, int nsteps)
     return NS_OK;
 }
 
-// A split-precision stage kernel whose TMA wait gave up leaves its error word
-// set; it is reported (and cleared) at the next synchronisation.
-static int check_split_err(ns_ctx *c)
+// A stage kernel whose TMA wait gave up leaves the error word set; it is
+// reported (and cleared) at the next synchronisation.
+static int check_kernel_err(ns_ctx *c)
 {
-    if (!c->split || !c->sp.err) return NS_OK;
+    if (!c->d_err) return NS_OK;
     int h = 0;
-    NS_CUDA(c, cudaMemcpyAsync(&h, c->sp.err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    NS_CUDA(c, cudaMemcpyAsync(&h, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     NS_CUDA(c, cudaStreamSynchronize(c->stream));
     if (!h) return NS_OK;
-    NS_CUDA(c, cudaMemsetAsync(c->sp.err, 0, sizeof(int), c->stream));
+    NS_CUDA(c, cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream));
     NS_CUDA(c, cudaStreamSynchronize(c->stream));
-    return set_err(c, NS_ERR_TIMEOUT, "a split-precision stage kernel timed out waiting for its TMA tile");
+    return set_err(c, NS_ERR_TIMEOUT, "a stage kernel timed out waiting for its TMA tile");
 }
 
 int ns_synchronize(ns_ctx *c)
@@ -879,7 +918,7 @@ int ns_synchronize(ns_ctx *c)
     if (!c) return set_err(nullptr, NS_ERR_PARAM, "ns_synchronize: NULL context");
     NS_CUDA(c, cudaSetDevice(c->dev));
     NS_CUDA(c, cudaStreamSynchronize(c->stream));
-    return check_split_err(c);
+    return check_kernel_err(c);
 }
 
 int ns_rk_euler(ns_ctx *c, double *U, double t, int iter, int nk)
@@ -914,7 +953,7 @@ int ns_rk_euler(ns_ctx *c, double *U, double t, int iter, int nk)
     if (c->split) NS_CUDA(c, ns::launch_split_to_full(c, c->U, c->stream));
     NS_CUDA(c, ns::launch_soa_to_aos(c->U, hv, c->d, c->stream));
     NS_CUDA(c, cudaStreamSynchronize(c->stream));
-    return check_split_err(c);
+    return check_kernel_err(c);
 }
 
 int ns_get_probes(ns_ctx *c, int np, const int32_t *pi, const int32_t *pj, double *out)

@@ -53,16 +53,24 @@ constexpr int kFilterPf = 8;
 // f points at position q of a line of length n and stride st; c = the 8
 // coefficients of position q.
 // ---------------------------------------------------------------------------
+// Interior 7-point DRP sum c1*(f1-f-1) + c2*(f2-f-2) + c3*(f3-f-3) along
+// stride st (global memory or a shared-memory tile: the same operations in
+// the same order, so both give identical bits).
+template <typename S>
+__device__ __forceinline__ double dint(const double *__restrict__ f, S st,
+                                       const double *__restrict__ c)
+{
+    const double c1 = c[4], c2 = c[5], c3 = c[6];
+    double r = c1 * (f[st] - f[-st]);
+    r = fma(c2, f[2 * st] - f[-2 * st], r);
+    r = fma(c3, f[3 * st] - f[-3 * st], r);
+    return r;
+}
+
 __device__ __forceinline__ double dline(const double *__restrict__ f, long long st, int q,
                                         int n, const double *__restrict__ c)
 {
-    if (q >= 3 && q < n - 3) {
-        const double c1 = c[4], c2 = c[5], c3 = c[6];
-        double r = c1 * (f[st] - f[-st]);
-        r = fma(c2, f[2 * st] - f[-2 * st], r);
-        r = fma(c3, f[3 * st] - f[-3 * st], r);
-        return r;
-    }
+    if (q >= 3 && q < n - 3) return dint(f, st, c);
     const int o0 = (q < 3) ? -q : (n - 7 - q);
     const double *g = f + (long long)o0 * st;
     double r = c[0] * g[0];
@@ -70,6 +78,12 @@ __device__ __forceinline__ double dline(const double *__restrict__ f, long long 
     for (int z = 1; z < 7; z++) r = fma(c[z], g[(long long)z * st], r);
     return r;
 }
+
+// Halo tile of the FP64 first-derivative kernel: a block of 32 x 8 points
+// reads a box of 40 x 14 doubles per plane starting 4 columns left (the box's
+// x coordinate times 8 bytes must be a multiple of 16) and 3 rows below.
+constexpr int kFirstBX = 32, kFirstBY = 8;
+constexpr int kFirstTileL = 4, kFirstTileW = 40, kFirstTileH = kFirstBY + 6;
 
 // Filter coefficients pre-multiplied by the filter strength.
 struct FilterCoef {
@@ -110,7 +124,6 @@ struct SplitState {
     int np = 3;
     float *q[2] = {nullptr, nullptr}; // perturbation ping-pong
     CUtensorMap qmap[2];              // TMA maps of q[0], q[1]: (imax, jmax, 4 + np) FP32
-    int *err = nullptr;               // set by a stage kernel whose TMA wait gave up
     float *xc = nullptr, *yc = nullptr;
     float *xcl = nullptr, *ycl = nullptr;  // FP64 table minus its FP32 rounding
     float *sigx = nullptr, *sigy = nullptr, *src = nullptr;
@@ -139,6 +152,13 @@ struct ns_ctx {
     double *stage_sin = nullptr;
     int *d_iter = nullptr;
     unsigned long long *d_count = nullptr;
+    int *d_err = nullptr;  // set by a kernel whose TMA wait gave up
+    // TMA maps of the FP64 stage kernels (box 40 x 14 x planes): U as
+    // (imax, jmax, nk) and the T plane of aux (imax, jmax, 1) for k_first;
+    // aux as (imax, jmax, AUX_COUNT) for k_update's derivative planes.
+    // Unset in ns_step_noalloc, whose kernels read global memory only.
+    bool fp64_maps = false;
+    CUtensorMap umap{}, tmap{}, amap{};
     double *probe_buf = nullptr;
     int probe_cap = 0;
     int32_t *probe_idx = nullptr;

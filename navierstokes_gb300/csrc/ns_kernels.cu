@@ -22,6 +22,7 @@
 
 #include "ns_fastmath.cuh"
 #include "ns_internal.cuh"
+#include "ns_tma.cuh"
 
 namespace ns {
 
@@ -88,34 +89,62 @@ __global__ void __launch_bounds__(256) k_prim(Dims d, const double *__restrict__
 // ---------------------------------------------------------------------------
 // k_first: first derivatives and everything pointwise built from them.
 // ---------------------------------------------------------------------------
-template <bool VISC, int NK>
+// With TMA, one elected thread loads the block's halo tile of U (and of T)
+// into shared memory and the interior stencils read it there; the closure
+// points near the domain edges read global memory.  Both give identical bits.
+template <bool VISC, int NK, bool TMA>
 __global__ void __launch_bounds__(256)
-    k_first(Dims d, const double *__restrict__ U, double *__restrict__ dudm,
-            double *__restrict__ dudn, double *__restrict__ aux,
+    k_first(const __grid_constant__ CUtensorMap umap, const __grid_constant__ CUtensorMap tmap,
+            int *__restrict__ err, Dims d, const double *__restrict__ U,
+            double *__restrict__ dudm, double *__restrict__ dudn, double *__restrict__ aux,
             const double *__restrict__ xcoef, const double *__restrict__ ycoef, Physics ph)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    constexpr int TW = kFirstTileW, TH = kFirstTileH;
+    __shared__ alignas(128) double su[TMA ? NK : 1][TMA ? TH : 1][TMA ? TW : 1];
+    __shared__ alignas(128) double sT[TMA && VISC ? TH : 1][TMA && VISC ? TW : 1];
+    __shared__ alignas(8) unsigned long long tbar;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int i = blockIdx.x * kFirstBX + tx;
+    const int j = blockIdx.y * kFirstBY + ty;
+    if constexpr (TMA) {
+        const bool lead = (tx == 0 && ty == 0);
+        if (lead) mbar_init(&tbar, 1);
+        __syncthreads();
+        if (lead) {
+            // boxes at (i0-4, j0-3): points outside the grid read as zero and
+            // are never used (their neighbours take the closure branch)
+            const int x0 = blockIdx.x * kFirstBX - kFirstTileL, y0 = blockIdx.y * kFirstBY - 3;
+            mbar_expect_tx(&tbar, (unsigned)(sizeof(su) + (VISC ? sizeof(sT) : 0)));
+            tma_load_3d(&su[0][0][0], &umap, x0, y0, 0, &tbar);
+            if (VISC) tma_load_3d(&sT[0][0], &tmap, x0, y0, 0, &tbar);
+        }
+        if (!mbar_wait_bounded(&tbar, 0, err)) return;
+    }
     if (i >= d.imax || j >= d.jmax) return;
     const long long idx = (long long)j * d.pitch + i;
     const long long P = d.plane, st = d.pitch;
     const double *cx = xcoef + kCoefStride * i;
     const double *cy = ycoef + kCoefStride * j;
+    const bool xin = TMA && i >= 3 && i < d.imax - 3;
+    const bool yin = TMA && j >= 3 && j < d.jmax - 3;
+    const int sr = ty + 3, sc = tx + kFirstTileL;
     double gx[NK], gy[NK];
 #pragma unroll
     for (int k = 0; k < NK; k++) {
         const double *f = U + k * P + idx;
-        gx[k] = dline(f, 1, i, d.imax, cx);
-        gy[k] = dline(f, st, j, d.jmax, cy);
+        const double *t = &su[TMA ? k : 0][TMA ? sr : 0][TMA ? sc : 0];
+        gx[k] = xin ? dint(t, 1, cx) : dline(f, 1, i, d.imax, cx);
+        gy[k] = yin ? dint(t, TW, cy) : dline(f, st, j, d.jmax, cy);
         dudm[k * P + idx] = gx[k];
         dudn[k * P + idx] = gy[k];
     }
     if (VISC) {
         // dT/dx, dT/dy (derivs.f90:25-26), mu(T), k(T) (coefficients.f90:27-59)
         const double *fT = aux + AUX_T * P + idx;
-        const double T = fT[0];
-        const double Tx = dline(fT, 1, i, d.imax, cx);
-        const double Ty = dline(fT, st, j, d.jmax, cy);
+        const double *t = &sT[TMA ? sr : 0][TMA ? sc : 0];
+        const double T = TMA ? t[0] : fT[0];
+        const double Tx = xin ? dint(t, 1, cx) : dline(fT, 1, i, d.imax, cx);
+        const double Ty = yin ? dint(t, TW, cy) : dline(fT, st, j, d.jmax, cy);
         const double x = ph.Tref * T;
         double L, y;
         fm::log_rcp_t(x, L, y);  // log(x), 1/x
@@ -135,7 +164,7 @@ __global__ void __launch_bounds__(256)
         aux[AUX_TAU3 * P + idx] = fma(mu2, gy[2], -(m23 * div));
     }
     if (NK >= 5) {
-        const double rho = U[idx];
+        const double rho = TMA ? su[0][sr][sc] : U[idx];
         aux[AUX_PSID * P + idx] = (rho * ph.alpha_cond) * (gx[NK - 1] + gy[NK - 1]);
     }
 }
@@ -145,9 +174,20 @@ __global__ void __launch_bounds__(256)
 // rk_steep on the interior (rk.f90:153-169) and bufferxy on the bands
 // (rk.f90:77-151), all points of the grid.
 // ---------------------------------------------------------------------------
-template <bool VISC, int NK, bool FIRST, bool SRC>
+// Planes of aux whose derivatives k_update takes: tau1, tau2, tau3, k dT/dx,
+// k dT/dy (viscous) and psiDiff (nk = 5), consecutive from kAuxTileZ0.
+template <bool VISC, int NK>
+constexpr int kAuxTileZ0 = VISC ? AUX_TAU1 : AUX_PSID;
+template <bool VISC, int NK>
+constexpr int kAuxTilePlanes = (VISC ? 5 : 0) + (NK >= 5 ? 1 : 0);
+
+// With TMA, the halo tile of those planes arrives in shared memory while the
+// pointwise inputs load; interior stencils read it there, closures read
+// global memory (identical bits either way).
+template <bool VISC, int NK, bool FIRST, bool SRC, bool TMA>
 __global__ void __launch_bounds__(256)
-    k_update(Dims d, double *__restrict__ U, double *__restrict__ W,
+    k_update(const __grid_constant__ CUtensorMap amap, int *__restrict__ err, Dims d,
+             double *__restrict__ U, double *__restrict__ W,
              const double *__restrict__ dudm, const double *__restrict__ dudn,
              const double *__restrict__ aux, const double *__restrict__ xcoef,
              const double *__restrict__ ycoef, const double *__restrict__ Ubase,
@@ -155,14 +195,44 @@ __global__ void __launch_bounds__(256)
              const double *__restrict__ src, const double *__restrict__ stage_sin, Physics ph,
              StageCoef sc)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    if (i >= d.imax || j >= d.jmax) return;
+    constexpr int TW = kFirstTileW, TH = kFirstTileH;
+    constexpr int NZ = TMA ? kAuxTilePlanes<VISC, NK> : 1;
+    static_assert(!TMA || kAuxTilePlanes<VISC, NK> > 0, "no aux tile to load");
+    // sa[z] = aux plane kAuxTileZ0 + z
+    __shared__ alignas(128) double sa[NZ][TMA ? TH : 1][TMA ? TW : 1];
+    __shared__ alignas(8) unsigned long long tbar;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int i = blockIdx.x * kFirstBX + tx;
+    const int j = blockIdx.y * kFirstBY + ty;
+    const bool lead = (tx == 0 && ty == 0);
+    if constexpr (TMA) {
+        if (lead) mbar_init(&tbar, 1);
+        __syncthreads();
+        if (lead) {
+            mbar_expect_tx(&tbar, (unsigned)sizeof(sa));
+            tma_load_3d(&sa[0][0][0], &amap, blockIdx.x * kFirstBX - kFirstTileL,
+                        blockIdx.y * kFirstBY - 3, kAuxTileZ0<VISC, NK>, &tbar);
+        }
+    }
+    const bool valid = i < d.imax && j < d.jmax;
     const long long idx = (long long)j * d.pitch + i;
     const long long P = d.plane, st = d.pitch;
     double u[NK];
+    if (valid) {
 #pragma unroll
-    for (int k = 0; k < NK; k++) u[k] = U[k * P + idx];
+        for (int k = 0; k < NK; k++) u[k] = U[k * P + idx];
+    }
+    // every thread waits, so no block exits with its tile load in flight
+    if constexpr (TMA)
+        if (!mbar_wait_bounded(&tbar, 0, err)) return;
+    if (!valid) return;
+    const bool xin = TMA && i >= 3 && i < d.imax - 3;
+    const bool yin = TMA && j >= 3 && j < d.jmax - 3;
+    const int sr = ty + 3, scol = tx + kFirstTileL;
+    // tile point of aux plane `a` at this thread's point
+    auto tp = [&](int a) {
+        return &sa[TMA ? a - kAuxTileZ0<VISC, NK> : 0][TMA ? sr : 0][TMA ? scol : 0];
+    };
 
     const bool interior = (i > 0) && (i < d.imax - 1) && (j > 0) && (j < d.jmax - 1);
     if (interior) {
@@ -205,16 +275,22 @@ __global__ void __launch_bounds__(256)
             const double *t1 = aux + AUX_TAU1 * P + idx;
             const double *t2 = aux + AUX_TAU2 * P + idx;
             const double *t3 = aux + AUX_TAU3 * P + idx;
-            const double dt1x = dline(t1, 1, i, d.imax, cx);
-            const double dt2x = dline(t2, 1, i, d.imax, cx);
-            const double dt2y = dline(t2, st, j, d.jmax, cy);
-            const double dt3y = dline(t3, st, j, d.jmax, cy);
-            const double d2T = dline(aux + AUX_KTX * P + idx, 1, i, d.imax, cx) +
-                               dline(aux + AUX_KTY * P + idx, st, j, d.jmax, cy);
+            const double *s1 = tp(AUX_TAU1), *s2 = tp(AUX_TAU2), *s3 = tp(AUX_TAU3);
+            const double dt1x = xin ? dint(s1, 1, cx) : dline(t1, 1, i, d.imax, cx);
+            const double dt2x = xin ? dint(s2, 1, cx) : dline(t2, 1, i, d.imax, cx);
+            const double dt2y = yin ? dint(s2, TW, cy) : dline(t2, st, j, d.jmax, cy);
+            const double dt3y = yin ? dint(s3, TW, cy) : dline(t3, st, j, d.jmax, cy);
+            const double dkx = xin ? dint(tp(AUX_KTX), 1, cx)
+                                   : dline(aux + AUX_KTX * P + idx, 1, i, d.imax, cx);
+            const double dky = yin ? dint(tp(AUX_KTY), TW, cy)
+                                   : dline(aux + AUX_KTY * P + idx, st, j, d.jmax, cy);
+            const double d2T = dkx + dky;
             const double rv = ph.inv_re * ri;
             a2 = fma(-rv, dt1x + dt2y, a2);
             a3 = fma(-rv, dt2x + dt3y, a3);
-            const double tau1 = t1[0], tau2 = t2[0], tau3 = t3[0];
+            const double tau1 = TMA ? s1[0] : t1[0];
+            const double tau2 = TMA ? s2[0] : t2[0];
+            const double tau3 = TMA ? s3[0] : t3[0];
             double phi = gx[1] * tau1;
             phi = fma(gx[2], tau2, phi);
             phi = fma(gy[1], tau2, phi);
@@ -228,7 +304,9 @@ __global__ void __launch_bounds__(256)
         if (NK >= 5) {
             // DUDT(5), :94-95
             const double *pd = aux + AUX_PSID * P + idx;
-            const double d2p = dline(pd, 1, i, d.imax, cx) + dline(pd, st, j, d.jmax, cy);
+            const double *sp = tp(AUX_PSID);
+            const double d2p = (xin ? dint(sp, 1, cx) : dline(pd, 1, i, d.imax, cx)) +
+                               (yin ? dint(sp, TW, cy) : dline(pd, st, j, d.jmax, cy));
             double a5 = uu * gx[NK - 1];
             a5 = fma(vv, gy[NK - 1], a5);
             a5 = fma(-(ph.inv_pe * ri), d2p, a5);
@@ -569,22 +647,39 @@ static cudaError_t launch_kernel_t(ns_ctx *c, int cls, int stage, cudaStream_t s
         k_prim<<<grd, blk, 0, s>>>(d, c->U, c->aux, c->phys.gamma);
         break;
     case NS_KC_FIRST:
-        k_first<VISC, NK><<<grd, blk, 0, s>>>(d, c->U, c->dudm, c->dudn, c->aux, c->xcoef,
-                                              c->ycoef, c->phys);
+        if (c->fp64_maps)
+            k_first<VISC, NK, true><<<grd, blk, 0, s>>>(c->umap, c->tmap, c->d_err, d, c->U,
+                                                        c->dudm, c->dudn, c->aux, c->xcoef,
+                                                        c->ycoef, c->phys);
+        else
+            k_first<VISC, NK, false><<<grd, blk, 0, s>>>(c->umap, c->tmap, c->d_err, d, c->U,
+                                                         c->dudm, c->dudn, c->aux, c->xcoef,
+                                                         c->ycoef, c->phys);
         break;
     case NS_KC_UPDATE: {
         StageCoef sc{c->alpha[stage], c->beta[stage], stage};
         const bool src = c->src != nullptr;
-#define NS_UPD(FIRST, SRC)                                                                     \
-    k_update<VISC, NK, FIRST, SRC><<<grd, blk, 0, s>>>(d, c->U, c->W, c->dudm, c->dudn,        \
-                                                       c->aux, c->xcoef, c->ycoef, c->Ubase,   \
-                                                       c->sigx, c->sigy, c->src, c->stage_sin, \
-                                                       c->phys, sc)
+        constexpr bool has_tile = kAuxTilePlanes<VISC, NK> > 0;
+        const bool tma = has_tile && c->fp64_maps;
+#define NS_UPD(FIRST, SRC, TMA)                                                                \
+    k_update<VISC, NK, FIRST, SRC, TMA><<<grd, blk, 0, s>>>(                                   \
+        c->amap, c->d_err, d, c->U, c->W, c->dudm, c->dudn, c->aux, c->xcoef, c->ycoef,        \
+        c->Ubase, c->sigx, c->sigy, c->src, c->stage_sin, c->phys, sc)
+#define NS_UPD2(FIRST, SRC)                             \
+    do {                                                \
+        if constexpr (has_tile) {                       \
+            if (tma) NS_UPD(FIRST, SRC, has_tile);      \
+            else NS_UPD(FIRST, SRC, false);             \
+        } else {                                        \
+            NS_UPD(FIRST, SRC, false);                  \
+        }                                               \
+    } while (0)
         if (stage == 0) {
-            if (src) NS_UPD(true, true); else NS_UPD(true, false);
+            if (src) NS_UPD2(true, true); else NS_UPD2(true, false);
         } else {
-            if (src) NS_UPD(false, true); else NS_UPD(false, false);
+            if (src) NS_UPD2(false, true); else NS_UPD2(false, false);
         }
+#undef NS_UPD2
 #undef NS_UPD
         break;
     }

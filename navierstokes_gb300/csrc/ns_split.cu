@@ -26,6 +26,7 @@
 // bit operations (IEEE-754 layouts, round to nearest even): on GB300 the F2F
 // instructions run on the FP64 pipe, which is about 60x slower than FP32.
 #include "ns_internal.cuh"
+#include "ns_tma.cuh"
 
 namespace ns {
 
@@ -105,57 +106,6 @@ constexpr int kSH = kTY + 2 * kH;
 // block (its x coordinate times 4 bytes must be a multiple of 16) and spans
 // 40 columns (a multiple of 16 bytes): i0-4 .. i0+35 covers the halo of 3.
 constexpr int kTL = 4, kSW = 40;
-
-// ---------------------------------------------------------------------------
-// TMA: one cp.async.bulk.tensor per block brings the whole halo tile of every
-// plane into shared memory; an mbarrier counts its bytes.  Every wait on the
-// barrier is bounded: a block that gives up sets the context's error word
-// and returns (the host reports NS_ERR_TIMEOUT).
-// ---------------------------------------------------------------------------
-constexpr long long kTmaSpinLimit = 1LL << 24;
-
-__device__ __forceinline__ unsigned smem_addr(const void *p)
-{
-    return (unsigned)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
-                 : "memory");
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
-                 "r"(bytes)
-                 : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity)
-{
-    unsigned done;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(done)
-        : "r"(smem_addr(bar)), "r"(parity)
-        : "memory");
-    return done != 0;
-}
-
-__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int x, int y, int z,
-                                            unsigned long long *bar)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-        " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_addr(dst)),
-        "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(z),
-        "r"(smem_addr(bar))
-        : "memory");
-}
 
 // One-sided closure, written as sum_z c_z*(f_z - f_q): the closure
 // coefficients sum to zero, and in this form a constant field gives exactly
@@ -265,15 +215,7 @@ __global__ void __launch_bounds__(256, 4)
             for (int k = 0; k < 4; k++) wold[h][k] = ok ? W[k * d.plane + didx] : 0.0;
         }
     }
-    {
-        long long spins = 0;
-        while (!mbar_try_wait(&tbar, 0)) {
-            if (++spins > kTmaSpinLimit) {
-                if (lead) atomicExch(err, 1);
-                return;
-            }
-        }
-    }
+    if (!mbar_wait_bounded(&tbar, 0, err)) return;
     const int i = i0 + tx;
     if (i >= d.imax) return;
     const float *cxp = xc + kCoefStride * i;
@@ -923,7 +865,7 @@ static cudaError_t launch_split_np(ns_ctx *c, int cls, int stage, cudaStream_t s
         const bool src = sp.src != nullptr;
 #define NS_SPL(FIRST, SRC)                                                                      \
     k_split_stage<NP, FIRST, SRC><<<grd, blk, 0, s>>>(                                          \
-        sp.qmap[stage & 1], sp.err, d, sp.fpitch, qa, qb, c->W, sp.xc, sp.yc, sp.xcl, sp.ycl,   \
+        sp.qmap[stage & 1], c->d_err, d, sp.fpitch, qa, qb, c->W, sp.xc, sp.yc, sp.xcl, sp.ycl,   \
         sp.mean, sp.sigx, sp.sigy, sp.src, c->stage_sin, (float)c->p.dt, c->alpha[stage],        \
         c->beta[stage], stage)
         if (stage == 0) {
