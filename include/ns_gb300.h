@@ -225,6 +225,14 @@ NS_API int ns_fp64_peak(int device, double *tflops);
  * x[0..n) into y[0..n) (host arrays). */
 NS_API int ns_math_eval(int fn, const double *x, double *y, int n, int device);
 
+/* Library diagnostic, no counterpart in the reference: mu(T) and k(T) of the
+ * transport law (coefficients.f90:27-59, divided by mu0 and k0) exactly as
+ * the context's first-derivative kernel evaluates them (its piecewise
+ * polynomial table, or exp and log outside the table's range), for
+ * T[0..n) into mu[0..n), k[0..n) (host arrays).  NS_ERR_STATE for an
+ * inviscid context. */
+NS_API int ns_transport_eval(ns_ctx *ctx, const double *T, double *mu, double *k, int n);
+
 /*
  * Batched sweeps: many independent Euler instances (inviscid = 1, nk = 4,
  * base flow uniform in x with v = 0 and uniform p; each with its own size,

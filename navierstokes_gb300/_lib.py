@@ -58,6 +58,7 @@ SIGNATURES = [
     ("ns_kernel_name", C.c_char_p, [C.c_int]),
     ("ns_fp64_peak", C.c_int, [C.c_int, C.POINTER(C.c_double)]),
     ("ns_math_eval", C.c_int, [C.c_int, _VP, _VP, C.c_int, C.c_int]),
+    ("ns_transport_eval", C.c_int, [_VP, _VP, _VP, _VP, C.c_int]),
     ("ns_step_noalloc", C.c_int, [_VP, _VP, C.c_int64, C.c_int, C.c_int, _VP]),
     ("ns_batch_create", C.c_int, [_VP, C.c_int, C.c_int, C.POINTER(_VP)]),
     ("ns_batch_destroy", None, [_VP]),

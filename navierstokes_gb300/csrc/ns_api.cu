@@ -287,7 +287,7 @@ void free_all(ns_ctx *c)
     if (c->step_exec) cudaGraphExecDestroy(c->step_exec);
     double *bufs[] = {c->U,    c->U2,   c->W,     c->dudm, c->dudn, c->aux,
                       c->Ubase, c->src, c->xcoef, c->ycoef, c->sigx, c->sigy,
-                      c->rhob, c->psib, c->stage_sin, c->probe_buf, c->rec_buf,
+                      c->rhob, c->psib, c->stage_sin, c->trtab, c->probe_buf, c->rec_buf,
                       c->vx, c->vy, c->omega};
     for (double *b : bufs)
         if (b) cudaFree(b);
@@ -568,6 +568,63 @@ void build_line_coef(std::vector<double> &tab, int n, double h, const double *me
 {
     build_coef(tab, n, h, mesh, D, metric_mode);
 }
+
+// mu(T) = exp(g_mi(Tref T) - g_mi(Tref)) and k(T) likewise, with
+// g(x) = A ln x + B/x + C/x^2 + D (coefficients.f90:27-59; the division by
+// mu0 and k0 of coefficients.f90 is the subtraction of g(Tref)).  Each piece
+// [t0, t0 + h) is interpolated at the kTrDeg+1 Chebyshev nodes in long
+// double; its Chebyshev series is converted to powers of s = (T - t0)/h and
+// then of u = T - t0 (h a power of two, so the scaling is exact).  With
+// h = t0/256 the interpolation error is far below the rounding of the
+// evaluation: for the N2 fit, mu and k evaluated in double are within
+// 2.3e-16 relative of the exact law over T in [1/4, 8) (below 1/4 the fit's
+// C/x^2 term makes k too steep for degree 5, so the table starts there).
+void build_transport_table(std::vector<double> &tab, double Tref, const double *a_mi,
+                           const double *a_k)
+{
+    constexpr int n = kTrDeg + 1;
+    tab.assign((size_t)kTrPieces * kTrStride, 0.0);
+    const long double pi = 3.141592653589793238462643383279502884L;
+    auto g = [](const double *a, long double x) {
+        return (long double)a[0] * std::log(x) + (long double)a[1] / x +
+               (long double)a[2] / (x * x) + (long double)a[3];
+    };
+    const long double tr = Tref;
+    const long double g0[2] = {g(a_mi, tr), g(a_k, tr)};
+    const double *coef[2] = {a_mi, a_k};
+    long double th[n], sn[n];
+    for (int i = 0; i < n; i++) {
+        th[i] = (2 * i + 1) * pi / (2 * n);
+        sn[i] = (1.0L - std::cos(th[i])) / 2;  // node in [0, 1]
+    }
+    // powers of s in T_m(2s - 1): T_0 = 1, T_1 = 2s - 1, T_m+1 = 2(2s-1)T_m - T_m-1
+    long double cm[n][n] = {};
+    cm[0][0] = 1;
+    cm[1][0] = -1;
+    cm[1][1] = 2;
+    for (int m = 1; m + 1 < n; m++)
+        for (int k = 0; k < n; k++)
+            cm[m + 1][k] = 2 * (2 * (k > 0 ? cm[m][k - 1] : 0.0L) - cm[m][k]) - cm[m - 1][k];
+    for (int piece = 0; piece < kTrPieces; piece++) {
+        const int e = kTrEmin + piece / 256, j = piece % 256;
+        const long double t0 = std::ldexp(1.0L + j / 256.0L, e);
+        const long double h = std::ldexp(1.0L, e - 8);
+        for (int f = 0; f < 2; f++) {
+            long double v[n], a[n] = {}, b[n] = {};
+            for (int i = 0; i < n; i++) v[i] = std::exp(g(coef[f], tr * (t0 + sn[i] * h)) - g0[f]);
+            // 2s - 1 = -cos(th_i), so T_m(2s_i - 1) = (-1)^m cos(m th_i)
+            for (int m = 0; m < n; m++) {
+                long double acc = 0;
+                for (int i = 0; i < n; i++) acc += v[i] * std::cos(m * th[i]);
+                a[m] = ((m & 1) ? -acc : acc) * (m == 0 ? 1.0L : 2.0L) / n;
+            }
+            for (int k = 0; k < n; k++)
+                for (int m = 0; m < n; m++) b[k] += a[m] * cm[m][k];
+            double *out = &tab[(size_t)piece * kTrStride + (size_t)f * n];
+            for (int k = 0; k < n; k++) out[k] = (double)std::ldexp(b[k], -k * (e - 8));
+        }
+    }
+}
 }  // namespace ns
 
 namespace ns {
@@ -687,6 +744,20 @@ int ns_create(const ns_params *p, ns_ctx **out)
     NS_TRY(dalloc(c, &c->d_count, 1));
     NS_TRY(dalloc(c, &c->d_err, 1));
     if (p->source_mode != NS_SRC_NONE) NS_TRY(dalloc(c, &c->src, P));
+    if (c->visc) {
+        NS_TRY(dalloc(c, &c->trtab, (size_t)ns::kTrPieces * ns::kTrStride));
+        std::vector<double> tab;
+        const double ami[4] = {p->A_mi, p->B_mi, p->C_mi, p->D_mi};
+        const double ak[4] = {p->A_k, p->B_k, p->C_k, p->D_k};
+        ns::build_transport_table(tab, p->Tref, ami, ak);
+        e = cudaMemcpyAsync(c->trtab, tab.data(), tab.size() * sizeof(double),
+                            cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) {
+            rc = cuda_err(c, e, "transport-law table");
+            goto fail;
+        }
+    }
     NS_TRY(make_fp64_maps(c));
 
     {

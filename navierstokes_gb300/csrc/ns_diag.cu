@@ -2,6 +2,7 @@
 //
 // ns_math_eval: the transport law's exp, log and 1/x (ns_fastmath.cuh) on
 // host arrays, for testing them against the library functions.
+// ns_transport_eval: mu(T), k(T) as a context's k_first evaluates them.
 //
 // ns_fp64_peak: the FP64 FMA throughput of a device, measured with a
 // register-only DFMA loop (8 independent chains per thread, 4 blocks of 256
@@ -78,6 +79,26 @@ extern "C" int ns_math_eval(int fn, const double *x, double *y, int n, int devic
     if (cudaMemcpy(d, x, (size_t)n * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
         ns::launch_math_eval(fn, d, d + n, n, 0) != cudaSuccess ||
         cudaMemcpy(y, d + n, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
+        rc = NS_ERR_CUDA;
+    cudaFree(d);
+    return rc;
+}
+
+extern "C" int ns_transport_eval(ns_ctx *c, const double *T, double *mu, double *k, int n)
+{
+    if (!c || n < 0 || (n > 0 && (!T || !mu || !k))) return NS_ERR_PARAM;
+    if (!c->visc) return NS_ERR_STATE;
+    if (n == 0) return NS_OK;
+    if (cudaSetDevice(c->dev) != cudaSuccess) return NS_ERR_CUDA;
+    double *d = nullptr;
+    if (cudaMalloc(&d, 3 * (size_t)n * sizeof(double)) != cudaSuccess) return NS_ERR_OOM;
+    int rc = NS_OK;
+    const size_t bytes = (size_t)n * sizeof(double);
+    if (cudaMemcpyAsync(d, T, bytes, cudaMemcpyHostToDevice, c->stream) != cudaSuccess ||
+        ns::launch_transport_eval(c, d, d + n, d + 2 * (size_t)n, n, c->stream) != cudaSuccess ||
+        cudaMemcpyAsync(mu, d + n, bytes, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+        cudaMemcpyAsync(k, d + 2 * (size_t)n, bytes, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+        cudaStreamSynchronize(c->stream) != cudaSuccess)
         rc = NS_ERR_CUDA;
     cudaFree(d);
     return rc;

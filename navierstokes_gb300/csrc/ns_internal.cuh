@@ -85,6 +85,16 @@ __device__ __forceinline__ double dline(const double *__restrict__ f, long long 
 constexpr int kFirstBX = 32, kFirstBY = 8;
 constexpr int kFirstTileL = 4, kFirstTileW = 40, kFirstTileH = kFirstBY + 6;
 
+// Transport law mu(T), k(T) (coefficients.f90:27-59) as piecewise
+// polynomials in T: T = 2^e (1 + (j + f)/256), e in [kTrEmin, kTrEmin +
+// kTrOctaves), j the top 8 fraction bits; piece (e, j) holds kTrDeg+1
+// coefficients of mu then of k in u = T - 2^e (1 + j/256) (exact, by
+// Sterbenz), Chebyshev interpolants of degree 5 on the piece.  T outside
+// that range takes the exp/log path.
+constexpr int kTrEmin = -2, kTrOctaves = 5, kTrDeg = 5;
+constexpr int kTrPieces = kTrOctaves * 256;
+constexpr int kTrStride = 2 * (kTrDeg + 1);  // doubles per piece
+
 // Filter coefficients pre-multiplied by the filter strength.
 struct FilterCoef {
     double c0;       // 1 - sigmaf*df(0)
@@ -150,6 +160,7 @@ struct ns_ctx {
     double *xcoef = nullptr, *ycoef = nullptr;
     double *sigx = nullptr, *sigy = nullptr, *rhob = nullptr, *psib = nullptr;
     double *stage_sin = nullptr;
+    double *trtab = nullptr;  // kTrPieces x kTrStride (viscous); null: exp/log path
     int *d_iter = nullptr;
     unsigned long long *d_count = nullptr;
     int *d_err = nullptr;  // set by a kernel whose TMA wait gave up
@@ -207,6 +218,14 @@ void build_line_coef(std::vector<double> &tab, int n, double h, const double *me
 // device, outside stream capture.
 cudaError_t ensure_math_tables(int device);
 cudaError_t launch_math_eval(int fn, const double *x, double *y, int n, cudaStream_t s);
+// mu(T) and k(T) of the transport law as k_first evaluates them (table or
+// exp/log path) (ns_kernels.cu)
+cudaError_t launch_transport_eval(const ns_ctx *c, const double *T, double *mu, double *k, int n,
+                                  cudaStream_t s);
+// The piecewise-polynomial table of mu(T), k(T) for these constants
+// (ns_api.cu).
+void build_transport_table(std::vector<double> &tab, double Tref, const double *a_mi,
+                           const double *a_k);
 // NS_LAYOUT_ROWS: rows[k + nk*j] -> every point of row j of plane k (ns_output.cu)
 cudaError_t launch_rows_to_planes(const double *rows, double *planes, const Dims &d,
                                   cudaStream_t s);

@@ -69,6 +69,54 @@ cudaError_t launch_math_eval(int fn, const double *x, double *y, int n, cudaStre
     return cudaGetLastError();
 }
 
+// mu(T) and k(T), 1/mu0 and 1/k0 included (coefficients.f90:27-59): from
+// the piecewise-polynomial table when T lies in its range (11 FP64
+// instructions), else by the table-driven log, 1/x and exp (43).
+__device__ __forceinline__ void transport(double T, const double *__restrict__ trtab,
+                                          const Physics &ph, double &mu, double &kc)
+{
+    const long long bt = __double_as_longlong(T);
+    const int e = (int)(bt >> 52) - 1023;  // the exponent when T > 0
+    if (trtab && bt > 0 && e >= kTrEmin && e < kTrEmin + kTrOctaves) {
+        const int piece = ((e - kTrEmin) << 8) | (int)((bt >> 44) & 255);
+        // T minus the piece's left end: the same exponent, so exact
+        const double u = T - __longlong_as_double(bt & ~((1LL << 44) - 1));
+        const double2 *c = reinterpret_cast<const double2 *>(trtab + (size_t)piece * kTrStride);
+        const double2 m01 = __ldg(c), m23 = __ldg(c + 1), m45 = __ldg(c + 2);
+        const double2 k01 = __ldg(c + 3), k23 = __ldg(c + 4), k45 = __ldg(c + 5);
+        mu = fma(fma(fma(fma(fma(m45.y, u, m45.x), u, m23.y), u, m23.x), u, m01.y), u, m01.x);
+        kc = fma(fma(fma(fma(fma(k45.y, u, k45.x), u, k23.y), u, k23.x), u, k01.y), u, k01.x);
+        return;
+    }
+    const double x = ph.Tref * T;
+    double L, y;
+    fm::log_rcp_t(x, L, y);  // log(x), 1/x
+    // 1/mu0 and 1/k0 enter as log(1/mu0) + D, log(1/k0) + D (Physics)
+    const double amu = fma(ph.A_mi, L, fma(fma(ph.C_mi, y, ph.B_mi), y, ph.D_mi_s));
+    const double ak = fma(ph.A_k, L, fma(fma(ph.C_k, y, ph.B_k), y, ph.D_k_s));
+    mu = fm::exp_t(amu);
+    kc = fm::exp_t(ak);
+}
+
+__global__ void k_transport_eval(const double *__restrict__ T, const double *__restrict__ trtab,
+                                 Physics ph, double *__restrict__ mu, double *__restrict__ k,
+                                 int n)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    double m, kc;
+    transport(T[q], trtab, ph, m, kc);
+    mu[q] = m;
+    k[q] = kc;
+}
+
+cudaError_t launch_transport_eval(const ns_ctx *c, const double *T, double *mu, double *k, int n,
+                                  cudaStream_t s)
+{
+    k_transport_eval<<<(n + 255) / 256, 256, 0, s>>>(T, c->trtab, c->phys, mu, k, n);
+    return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------------------
 // k_prim: T and 1/rho (rhs.f90:20), pointwise.
 // ---------------------------------------------------------------------------
@@ -97,7 +145,8 @@ __global__ void __launch_bounds__(256)
     k_first(const __grid_constant__ CUtensorMap umap, const __grid_constant__ CUtensorMap tmap,
             int *__restrict__ err, Dims d, const double *__restrict__ U,
             double *__restrict__ dudm, double *__restrict__ dudn, double *__restrict__ aux,
-            const double *__restrict__ xcoef, const double *__restrict__ ycoef, Physics ph)
+            const double *__restrict__ xcoef, const double *__restrict__ ycoef,
+            const double *__restrict__ trtab, Physics ph)
 {
     constexpr int TW = kFirstTileW, TH = kFirstTileH;
     __shared__ alignas(128) double su[TMA ? NK : 1][TMA ? TH : 1][TMA ? TW : 1];
@@ -145,14 +194,8 @@ __global__ void __launch_bounds__(256)
         const double T = TMA ? t[0] : fT[0];
         const double Tx = xin ? dint(t, 1, cx) : dline(fT, 1, i, d.imax, cx);
         const double Ty = yin ? dint(t, TW, cy) : dline(fT, st, j, d.jmax, cy);
-        const double x = ph.Tref * T;
-        double L, y;
-        fm::log_rcp_t(x, L, y);  // log(x), 1/x
-        // 1/mu0 and 1/k0 enter as log(1/mu0) + D, log(1/k0) + D (Physics)
-        const double amu = fma(ph.A_mi, L, fma(fma(ph.C_mi, y, ph.B_mi), y, ph.D_mi_s));
-        const double ak = fma(ph.A_k, L, fma(fma(ph.C_k, y, ph.B_k), y, ph.D_k_s));
-        const double mu = fm::exp_t(amu);
-        const double kc = fm::exp_t(ak);
+        double mu, kc;
+        transport(T, trtab, ph, mu, kc);
         aux[AUX_KTX * P + idx] = Tx * kc;  // kdT (derivs.f90:48-56)
         aux[AUX_KTY * P + idx] = Ty * kc;
         // TAU_IJ (eqeuler.f90:37-39)
@@ -650,11 +693,11 @@ static cudaError_t launch_kernel_t(ns_ctx *c, int cls, int stage, cudaStream_t s
         if (c->fp64_maps)
             k_first<VISC, NK, true><<<grd, blk, 0, s>>>(c->umap, c->tmap, c->d_err, d, c->U,
                                                         c->dudm, c->dudn, c->aux, c->xcoef,
-                                                        c->ycoef, c->phys);
+                                                        c->ycoef, c->trtab, c->phys);
         else
             k_first<VISC, NK, false><<<grd, blk, 0, s>>>(c->umap, c->tmap, c->d_err, d, c->U,
                                                          c->dudm, c->dudn, c->aux, c->xcoef,
-                                                         c->ycoef, c->phys);
+                                                         c->ycoef, c->trtab, c->phys);
         break;
     case NS_KC_UPDATE: {
         StageCoef sc{c->alpha[stage], c->beta[stage], stage};

@@ -55,3 +55,45 @@ def test_special_values_follow_the_library(nslib):
         assert np.array_equal(np.isnan(g), np.isnan(w))
         ok = ~np.isnan(w)
         assert np.allclose(g[ok], w[ok], rtol=1e-15, atol=0.0)
+
+
+def test_transport_table(nslib):
+    """mu(T), k(T) as the first-derivative kernel evaluates them: the
+    piecewise-polynomial table over T in [1/4, 8), exp and log outside it,
+    against the law evaluated in extended precision."""
+    import ctypes as C
+
+    from navierstokes_gb300.cases import N2_FIT, acoustic_pulse_case
+    from navierstokes_gb300.solver import Solver
+
+    if np.finfo(np.longdouble).eps > 1e-18:
+        pytest.skip("numpy long double is not wider than double here")
+    case = acoustic_pulse_case(imax=32, jmax=32, nk=4, D=8, inviscid=False)
+    rng = np.random.default_rng(5)
+    inside = np.concatenate([rng.uniform(0.25, 8.0, 20000), 2.0 ** rng.uniform(-2, 3, 20000),
+                             [0.25, 0.5, 1.0, 2.0, 4.0, np.nextafter(8.0, 0.0),
+                              np.nextafter(0.25, 1.0), 1.0 + 2.0 ** -44]])
+    outside = np.array([0.1, 0.2, np.nextafter(0.25, 0.0), 8.0, 20.0, 0.05, 300.0])
+    T = np.ascontiguousarray(np.concatenate([inside, outside]))
+    mu, k = np.empty_like(T), np.empty_like(T)
+    with Solver(case) as s:
+        assert nslib.ns_transport_eval(s._ctx, T.ctypes.data, mu.ctypes.data, k.ctypes.data,
+                                       len(T)) == 0
+    ld = np.longdouble
+
+    def law(A, B, C_, D):
+        """exp(arg) and arg = g(Tref T) - g(Tref)"""
+        def g(x):
+            return ld(A) * np.log(x) + ld(B) / x + ld(C_) / (x * x) + ld(D)
+        arg = g(ld(case.Tref) * T.astype(ld)) - g(ld(case.Tref))
+        return np.exp(arg), np.abs(arg).astype(np.float64)
+
+    f = N2_FIT
+    n = len(inside)
+    for got, (ref, arg) in ((mu, law(f["A_mi"], f["B_mi"], f["C_mi"], f["D_mi"])),
+                            (k, law(f["A_k"], f["B_k"], f["C_k"], f["D_k"]))):
+        rel = np.abs((got.astype(ld) - ref) / ref).astype(np.float64)
+        assert rel[:n].max() <= 3e-16          # table: about 2 ulp
+        # exp/log path: the rounding of the exponent argument (about
+        # 1.1e-16 |arg| absolute) becomes relative error of exp, plus a few ulp
+        assert np.all(rel[n:] <= 2.2e-16 * (4.0 + arg[n:]))
