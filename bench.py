@@ -45,14 +45,14 @@ BYTES_PER_POINT = {"k_prim": 32, "k_first": 144, "k_update": 240, "k_filter_x": 
 # FP64 work per grid point of one launch, from the ncu instruction counts of
 # profiles/fp64_counts_ns_2048x2048.md (nk = 4, Navier-Stokes): flops (2 per
 # DFMA, 1 per DADD/DMUL) and FP64-pipe thread instructions.
-FP64_FLOP_PER_POINT = {"k_prim": 12.0, "k_first": 166.15, "k_update": 111.45,
+FP64_FLOP_PER_POINT = {"k_prim": 12.0, "k_first": 113.15, "k_update": 111.43,
                        "k_filter_x": 90.15, "k_filter_y": 90.15}
-FP64_INST_PER_POINT = {"k_prim": 7.0, "k_first": 112.03, "k_update": 74.82,
+FP64_INST_PER_POINT = {"k_prim": 7.0, "k_first": 81.03, "k_update": 71.84,
                        "k_filter_x": 58.56, "k_filter_y": 58.56}
 # DRAM bytes (read + write) per point of one launch from the same capture
 # (2048x2048), scaled to a launch by the number of points.
-TRAFFIC_PER_POINT = {"k_prim": 21.3, "k_first": 130.4, "k_update": 230.6,
-                     "k_filter_x": 61.8, "k_filter_y": 61.8}
+TRAFFIC_PER_POINT = {"k_prim": 21.3, "k_first": 129.9, "k_update": 230.5,
+                     "k_filter_x": 61.7, "k_filter_y": 61.7}
 FP64_PEAK_FALLBACK_TFLOPS = 1.19  # DFMA throughput measured on GB300 (profiles/fp64_peak.md)
 STEP_BYTES_FUSED_MIN = 1536  # compulsory bytes per point-step of a fused FP64 design, nk = 4
 
@@ -592,6 +592,13 @@ def run_ours(args, world, rank, local, pg):
                         "pipe_inst_per_s": ins * 1e9, "pipe_frac": ins / peak_ins,
                         "peak_source": "ns_fp64_peak(): DFMA loop measured live on this GPU",
                         "binding": "the FP64 pipe binds this kernel, not HBM"}
+        # nominal rate: 2 FP64 thread instructions per clock per SM at the
+        # maximum SM clock (the DFMA loop reaches about 1.7 on these parts)
+        nsm = torch.cuda.get_device_properties(local).multi_processor_count
+        if clocks.get("sm_max_mhz"):
+            nominal = 2.0 * nsm * clocks["sm_max_mhz"] * 1e6
+            roof["fp64"]["pipe_inst_per_s_nominal"] = nominal
+            roof["fp64"]["pipe_frac_nominal"] = ins * 1e9 / nominal
     step_bytes = STEP_BYTES_FUSED_MIN * case.points
     roof["step_hbm_frac_fused_min"] = step_bytes / (ms_step * 1e-3) / 1e9 / hbm_peak
 

@@ -57,10 +57,9 @@ constexpr int kFilterPf = 8;
 // stride st (global memory or a shared-memory tile: the same operations in
 // the same order, so both give identical bits).
 template <typename S>
-__device__ __forceinline__ double dint(const double *__restrict__ f, S st,
-                                       const double *__restrict__ c)
+__device__ __forceinline__ double dint(const double *__restrict__ f, S st, double c1, double c2,
+                                       double c3)
 {
-    const double c1 = c[4], c2 = c[5], c3 = c[6];
     double r = c1 * (f[st] - f[-st]);
     r = fma(c2, f[2 * st] - f[-2 * st], r);
     r = fma(c3, f[3 * st] - f[-3 * st], r);
@@ -70,7 +69,7 @@ __device__ __forceinline__ double dint(const double *__restrict__ f, S st,
 __device__ __forceinline__ double dline(const double *__restrict__ f, long long st, int q,
                                         int n, const double *__restrict__ c)
 {
-    if (q >= 3 && q < n - 3) return dint(f, st, c);
+    if (q >= 3 && q < n - 3) return dint(f, st, c[4], c[5], c[6]);
     const int o0 = (q < 3) ? -q : (n - 7 - q);
     const double *g = f + (long long)o0 * st;
     double r = c[0] * g[0];

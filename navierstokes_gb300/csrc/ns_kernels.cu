@@ -174,6 +174,8 @@ __global__ void __launch_bounds__(256)
     const long long P = d.plane, st = d.pitch;
     const double *cx = xcoef + kCoefStride * i;
     const double *cy = ycoef + kCoefStride * j;
+    const double cx1 = cx[4], cx2 = cx[5], cx3 = cx[6];
+    const double cy1 = cy[4], cy2 = cy[5], cy3 = cy[6];
     const bool xin = TMA && i >= 3 && i < d.imax - 3;
     const bool yin = TMA && j >= 3 && j < d.jmax - 3;
     const int sr = ty + 3, sc = tx + kFirstTileL;
@@ -182,8 +184,8 @@ __global__ void __launch_bounds__(256)
     for (int k = 0; k < NK; k++) {
         const double *f = U + k * P + idx;
         const double *t = &su[TMA ? k : 0][TMA ? sr : 0][TMA ? sc : 0];
-        gx[k] = xin ? dint(t, 1, cx) : dline(f, 1, i, d.imax, cx);
-        gy[k] = yin ? dint(t, TW, cy) : dline(f, st, j, d.jmax, cy);
+        gx[k] = xin ? dint(t, 1, cx1, cx2, cx3) : dline(f, 1, i, d.imax, cx);
+        gy[k] = yin ? dint(t, TW, cy1, cy2, cy3) : dline(f, st, j, d.jmax, cy);
         dudm[k * P + idx] = gx[k];
         dudn[k * P + idx] = gy[k];
     }
@@ -192,8 +194,8 @@ __global__ void __launch_bounds__(256)
         const double *fT = aux + AUX_T * P + idx;
         const double *t = &sT[TMA ? sr : 0][TMA ? sc : 0];
         const double T = TMA ? t[0] : fT[0];
-        const double Tx = xin ? dint(t, 1, cx) : dline(fT, 1, i, d.imax, cx);
-        const double Ty = yin ? dint(t, TW, cy) : dline(fT, st, j, d.jmax, cy);
+        const double Tx = xin ? dint(t, 1, cx1, cx2, cx3) : dline(fT, 1, i, d.imax, cx);
+        const double Ty = yin ? dint(t, TW, cy1, cy2, cy3) : dline(fT, st, j, d.jmax, cy);
         double mu, kc;
         transport(T, trtab, ph, mu, kc);
         aux[AUX_KTX * P + idx] = Tx * kc;  // kdT (derivs.f90:48-56)
@@ -314,23 +316,37 @@ __global__ void __launch_bounds__(256)
         }
         const double *cx = xcoef + kCoefStride * i;
         const double *cy = ycoef + kCoefStride * j;
+        const double cx1 = cx[4], cx2 = cx[5], cx3 = cx[6];
+        const double cy1 = cy[4], cy2 = cy[5], cy3 = cy[6];
+        // d/dx of aux plane ax (global: gax) plus d/dy of plane ay (gay): in
+        // the interior one FMA chain over both stencils from the tile (one
+        // addition fewer), at the closures the two sums of dline
+        auto dxy = [&](int ax, const double *gax, int ay, const double *gay) -> double {
+            if (xin && yin) {
+                const double *a = tp(ax), *b = tp(ay);
+                double r = cx1 * (a[1] - a[-1]);
+                r = fma(cx2, a[2] - a[-2], r);
+                r = fma(cx3, a[3] - a[-3], r);
+                r = fma(cy1, b[TW] - b[-TW], r);
+                r = fma(cy2, b[2 * TW] - b[-2 * TW], r);
+                r = fma(cy3, b[3 * TW] - b[-3 * TW], r);
+                return r;
+            }
+            return (xin ? dint(tp(ax), 1, cx1, cx2, cx3) : dline(gax, 1, i, d.imax, cx)) +
+                   (yin ? dint(tp(ay), TW, cy1, cy2, cy3) : dline(gay, st, j, d.jmax, cy));
+        };
         if (VISC) {
             const double *t1 = aux + AUX_TAU1 * P + idx;
             const double *t2 = aux + AUX_TAU2 * P + idx;
             const double *t3 = aux + AUX_TAU3 * P + idx;
             const double *s1 = tp(AUX_TAU1), *s2 = tp(AUX_TAU2), *s3 = tp(AUX_TAU3);
-            const double dt1x = xin ? dint(s1, 1, cx) : dline(t1, 1, i, d.imax, cx);
-            const double dt2x = xin ? dint(s2, 1, cx) : dline(t2, 1, i, d.imax, cx);
-            const double dt2y = yin ? dint(s2, TW, cy) : dline(t2, st, j, d.jmax, cy);
-            const double dt3y = yin ? dint(s3, TW, cy) : dline(t3, st, j, d.jmax, cy);
-            const double dkx = xin ? dint(tp(AUX_KTX), 1, cx)
-                                   : dline(aux + AUX_KTX * P + idx, 1, i, d.imax, cx);
-            const double dky = yin ? dint(tp(AUX_KTY), TW, cy)
-                                   : dline(aux + AUX_KTY * P + idx, st, j, d.jmax, cy);
-            const double d2T = dkx + dky;
+            const double dtau_u = dxy(AUX_TAU1, t1, AUX_TAU2, t2);  // dtau11/dx + dtau12/dy
+            const double dtau_v = dxy(AUX_TAU2, t2, AUX_TAU3, t3);  // dtau12/dx + dtau22/dy
+            const double d2T = dxy(AUX_KTX, aux + AUX_KTX * P + idx, AUX_KTY,
+                                   aux + AUX_KTY * P + idx);
             const double rv = ph.inv_re * ri;
-            a2 = fma(-rv, dt1x + dt2y, a2);
-            a3 = fma(-rv, dt2x + dt3y, a3);
+            a2 = fma(-rv, dtau_u, a2);
+            a3 = fma(-rv, dtau_v, a3);
             const double tau1 = TMA ? s1[0] : t1[0];
             const double tau2 = TMA ? s2[0] : t2[0];
             const double tau3 = TMA ? s3[0] : t3[0];
@@ -347,9 +363,7 @@ __global__ void __launch_bounds__(256)
         if (NK >= 5) {
             // DUDT(5), :94-95
             const double *pd = aux + AUX_PSID * P + idx;
-            const double *sp = tp(AUX_PSID);
-            const double d2p = (xin ? dint(sp, 1, cx) : dline(pd, 1, i, d.imax, cx)) +
-                               (yin ? dint(sp, TW, cy) : dline(pd, st, j, d.jmax, cy));
+            const double d2p = dxy(AUX_PSID, pd, AUX_PSID, pd);
             double a5 = uu * gx[NK - 1];
             a5 = fma(vv, gy[NK - 1], a5);
             a5 = fma(-(ph.inv_pe * ri), d2p, a5);
