@@ -861,6 +861,7 @@ constants:
         c->warm = filter_warmup(p->sigmaf);
         int nsm = 152;
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->dev);
+        c->nsm = nsm;
         c->fx_chunks = choose_chunks_fp64(d.jmax * d.nk, d.imax, c->warm, nsm);
         c->fy_chunks = choose_chunks_fp64(d.imax * d.nk, d.jmax, c->warm, nsm);
         if (c->split) {

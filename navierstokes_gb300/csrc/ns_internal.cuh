@@ -46,6 +46,9 @@ constexpr int kCoefStride = 8;
 // Points per block of the FP64 filter recurrences (loads issued one block
 // ahead).
 constexpr int kFilterPf = 8;
+// Warps per SM sub-partition of the FP64 filter sweeps (k_filter deals the
+// pass-2 work out in equal segments, one per warp).
+constexpr int kFilterWarpsPerSmsp = 2;
 
 // ---------------------------------------------------------------------------
 // DRP first derivative along a line (diff.f90:40-238 with the metric of
@@ -183,7 +186,8 @@ struct ns_ctx {
     ns::FilterCoef fx, fy;
     double ct[6], alpha[6], beta[6];
     int warm = 0;       // filter warm-up length (-1: serial sweeps)
-    int fx_chunks = 1, fy_chunks = 1;
+    int fx_chunks = 1, fy_chunks = 1;  // chunks per line of the adjoint's filter transposes
+    int nsm = 152;      // multiprocessors of the device
     bool visc = false;
     bool split = false;
     ns::SplitState sp;

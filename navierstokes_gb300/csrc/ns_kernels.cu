@@ -17,6 +17,7 @@
 //   k_filter<x>          lddfilterx as chunked recurrences  filtering.f90:9-96
 //   k_filter<y>          lddfiltery                         filtering.f90:98-190
 //   k_bc                 ccpml                              cc.f90:6-68
+#include <algorithm>
 #include <cmath>
 #include <mutex>
 
@@ -447,33 +448,17 @@ __device__ __forceinline__ void shift13(double *w, double v, double next)
     w[12] = next;
 }
 
-template <bool ALONG_Y>
-__global__ void __launch_bounds__(128)
-    k_filter(Dims d, const double *__restrict__ src, double *__restrict__ dst, int chunks,
-             int warm, FilterCoef fc)
+// Pass-2 positions [a, b) of one line (6 <= a < b <= n-6): a == 6 starts
+// exactly with pass 1 and writes its outputs, a later start runs `warm`
+// points of unfiltered history first (or starts exactly when that reaches
+// back to position 6); b == n-6 ends with pass 3.
+__device__ __forceinline__ void filter_piece(const double *__restrict__ s, double *__restrict__ o,
+                                             long long st, int n, int a, int b, int warm,
+                                             const FilterCoef &fc)
 {
-    const int nlines = ALONG_Y ? d.imax : d.jmax;
-    const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long total = (long long)nlines * d.nk * chunks;
-    if (gid >= total) return;
-    const int line = (int)(gid % nlines);
-    const int rest = (int)(gid / nlines);
-    const int k = rest % d.nk;
-    const int c = rest / d.nk;
-    const int n = ALONG_Y ? d.jmax : d.imax;
-    const long long st = ALONG_Y ? d.pitch : 1;
-    const long long base = (long long)k * d.plane + (ALONG_Y ? line : (long long)line * d.pitch);
-    const double *__restrict__ s = src + base;
-    double *__restrict__ o = dst + base;
-
-    const int len2 = n - 12;  // pass-2 positions 6 .. n-7
-    const int a = 6 + (int)(((long long)c * len2) / chunks);
-    const int b = 6 + (int)(((long long)(c + 1) * len2) / chunks);
-    const bool last = (c == chunks - 1);
-
     double w[13];
     int q;
-    if (c == 0 || warm < 0 || a - warm <= 6) {
+    if (a == 6 || warm < 0 || a - warm <= 6) {
         // exact start: pass 1 (filtering.f90:39-49 / :128-140)
 #pragma unroll
         for (int t = 0; t < 13; t++) w[t] = s[t * st];
@@ -485,7 +470,7 @@ __global__ void __launch_bounds__(128)
             v = fma(fc.bm1, w[p - 1], v);
             w[p] = v;
         }
-        if (c == 0) {
+        if (a == 6) {
 #pragma unroll
             for (int p = 0; p < 6; p++) o[p * st] = w[p];
         }
@@ -497,7 +482,7 @@ __global__ void __launch_bounds__(128)
     }
     // pass 2 (filtering.f90:69-79 / :161-171).  Blocks of kFilterPf points,
     // the next block's input loaded before the current block is filtered, so
-    // that a thread keeps kFilterPf loads in flight when few lines run.
+    // that a thread keeps kFilterPf loads in flight.
     double nx[kFilterPf];
 #pragma unroll
     for (int t = 0; t < kFilterPf; t++) {
@@ -524,7 +509,7 @@ __global__ void __launch_bounds__(128)
         if (q >= a) o[(long long)q * st] = v;
         shift13(w, v, (q + 7 < n) ? s[(long long)(q + 7) * st] : 0.0);
     }
-    if (last) {
+    if (b == n - 6) {
         // pass 3 (filtering.f90:84-94 / :176-188): w[0..11] = positions n-12..n-1
 #pragma unroll
         for (int x = 10; x >= 5; x--) {
@@ -537,6 +522,69 @@ __global__ void __launch_bounds__(128)
 #pragma unroll
         for (int x = 5; x < 12; x++) o[(long long)(n - 12 + x) * st] = w[x];
     }
+}
+
+// Work is dealt out in warp-lines: 32 adjacent lines of one variable (rows
+// j for x, columns i for y), one per lane, so a warp's loads and stores of a
+// position are 32 neighbouring lines and every lane takes the same branches.
+// The pass-2 positions of all warp-lines, laid end to end, are cut into equal
+// segments of `seg` positions, one per warp: a segment covers the end of one
+// warp-line and the start of the next, each piece with its own start (exact
+// or warm) and end (pass 3 or not).  Equal segments give every warp the same
+// work up to one warm-up, whatever the number of lines.
+template <bool ALONG_Y>
+__global__ void __launch_bounds__(128)
+    k_filter(Dims d, const double *__restrict__ src, double *__restrict__ dst, long long seg,
+             int warm, FilterCoef fc)
+{
+    const int lane = threadIdx.x & 31;
+    const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nlines = ALONG_Y ? d.imax : d.jmax;  // lines per variable
+    const int gpk = (nlines + 31) >> 5;            // warp-lines per variable
+    const int n = ALONG_Y ? d.jmax : d.imax;
+    const int len2 = n - 12;                       // pass-2 positions 6 .. n-7
+    const long long total = (long long)gpk * d.nk * len2;
+    const long long s0 = wid * seg;
+    const long long s1 = s0 + seg < total ? s0 + seg : total;
+    const long long st = ALONG_Y ? d.pitch : 1;
+    for (long long sp = s0; sp < s1;) {
+        const long long g = sp / len2;
+        const long long gend = (g + 1) * len2;
+        const long long e = s1 < gend ? s1 : gend;
+        const int k = (int)(g / gpk);
+        const int line = (int)(g % gpk) * 32 + lane;
+        if (line < nlines) {
+            const long long base =
+                (long long)k * d.plane + (ALONG_Y ? line : (long long)line * d.pitch);
+            filter_piece(src + base, dst + base, st, n, 6 + (int)(sp - g * len2),
+                         6 + (int)(e - g * len2), warm, fc);
+        }
+        sp = e;
+    }
+}
+
+// Launch shape of k_filter: nsm*4*kw warps (kw per SM sub-partition), fewer
+// when the segments would get shorter than the warm-up plus 6 on average;
+// whole warp-lines per warp when the warm-up is unbounded (warm < 0).
+static void filter_shape(int nlines, int n, int nk, int warm, int nsm, int kw, long long &seg,
+                         unsigned &blocks)
+{
+    const long long gtot = (long long)nk * ((nlines + 31) / 32);
+    const int len2 = n - 12;
+    const long long total = gtot * len2;
+    long long nw;
+    if (warm < 0) {
+        seg = len2;
+        nw = gtot;
+    } else {
+        nw = (long long)nsm * 4 * kw;
+        const long long maxw = gtot * std::max(1, len2 / (warm + 6));
+        if (nw > maxw) nw = maxw;
+        if (nw < 1) nw = 1;
+        seg = (total + nw - 1) / nw;
+        nw = (total + seg - 1) / seg;
+    }
+    blocks = (unsigned)((nw * 32 + 127) / 128);
 }
 
 // ---------------------------------------------------------------------------
@@ -741,15 +789,17 @@ static cudaError_t launch_kernel_t(ns_ctx *c, int cls, int stage, cudaStream_t s
         break;
     }
     case NS_KC_FILTER_X: {
-        const long long tx = (long long)d.jmax * d.nk * c->fx_chunks;
-        k_filter<false><<<(unsigned)((tx + 127) / 128), 128, 0, s>>>(d, c->U, c->U2,
-                                                                     c->fx_chunks, c->warm, c->fx);
+        long long seg;
+        unsigned nb;
+        filter_shape(d.jmax, d.imax, d.nk, c->warm, c->nsm, kFilterWarpsPerSmsp, seg, nb);
+        k_filter<false><<<nb, 128, 0, s>>>(d, c->U, c->U2, seg, c->warm, c->fx);
         break;
     }
     case NS_KC_FILTER_Y: {
-        const long long ty = (long long)d.imax * d.nk * c->fy_chunks;
-        k_filter<true><<<(unsigned)((ty + 127) / 128), 128, 0, s>>>(d, c->U2, c->U, c->fy_chunks,
-                                                                    c->warm, c->fy);
+        long long seg;
+        unsigned nb;
+        filter_shape(d.imax, d.jmax, d.nk, c->warm, c->nsm, kFilterWarpsPerSmsp, seg, nb);
+        k_filter<true><<<nb, 128, 0, s>>>(d, c->U2, c->U, seg, c->warm, c->fy);
         break;
     }
     case NS_KC_BC: {

@@ -141,15 +141,6 @@ int warmup(double sigmaf)
     return w < 36 ? 36 : w;
 }
 
-int chunks(int nlines_total, int n, int warm, int target)
-{
-    if (warm < 0) return 1;
-    int c = (target + nlines_total - 1) / nlines_total;
-    const int maxc = (n - 12) / (4 * (warm + 6));
-    if (c > maxc) c = maxc;
-    return c < 1 ? 1 : c;
-}
-
 __global__ void k_gauss_field(double *__restrict__ src, const double *__restrict__ m,
                               const double *__restrict__ n, ns::Dims d, double amplitude,
                               double m_pt, double n_pt, double r0, double ln2)
@@ -333,9 +324,7 @@ extern "C" int ns_step_noalloc(const ns_params *p, double *U, int64_t pitch, int
     c.warm = warmup(p->sigmaf);
     int nsm = 152;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    const int target = nsm * 4 * 2 * 32;
-    c.fx_chunks = chunks(d.jmax * nk, d.imax, c.warm, target);
-    c.fy_chunks = chunks(d.imax * nk, d.jmax, c.warm, target);
+    c.nsm = nsm;
 
     // the step, kernel by kernel (no graph: instantiating one allocates)
     int cls[ns::kMaxStepLaunches], stage[ns::kMaxStepLaunches];
