@@ -563,24 +563,26 @@ __global__ void __launch_bounds__(128)
     }
 }
 
-// Launch shape of k_filter: nsm*4*kw warps (kw per SM sub-partition), fewer
-// when the segments would get shorter than the warm-up plus 6 on average;
-// whole warp-lines per warp when the warm-up is unbounded (warm < 0).
+// Launch shape of k_filter: one warp per SM sub-partition, or kw when the
+// segments stay long against the warm-up (at least 8x; a second warp per
+// sub-partition hides latency but adds a warm-up to every segment); whole
+// warp-lines per warp when the warm-up is unbounded (warm < 0).  A warp
+// count just above a multiple of the sub-partitions would leave most of them
+// waiting for the few that run two warps, so the count is a multiple.
 static void filter_shape(int nlines, int n, int nk, int warm, int nsm, int kw, long long &seg,
                          unsigned &blocks)
 {
     const long long gtot = (long long)nk * ((nlines + 31) / 32);
     const int len2 = n - 12;
     const long long total = gtot * len2;
+    const long long S = 4LL * nsm;
     long long nw;
     if (warm < 0) {
         seg = len2;
         nw = gtot;
     } else {
-        nw = (long long)nsm * 4 * kw;
-        const long long maxw = gtot * std::max(1, len2 / (warm + 6));
-        if (nw > maxw) nw = maxw;
-        if (nw < 1) nw = 1;
+        const int k = (total / (kw * S) >= 8LL * (warm + 6)) ? kw : 1;
+        nw = k * S;
         seg = (total + nw - 1) / nw;
         nw = (total + seg - 1) / seg;
     }
