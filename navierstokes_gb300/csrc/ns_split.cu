@@ -575,14 +575,35 @@ __global__ void __launch_bounds__(128)
 
 // x filter: each warp owns 32 consecutive rows of one variable and one
 // chunk.  The old values a lane appends to its window (position q+7 at step
-// q) are staged 32 positions at a time through a [32][33] tile loaded with
-// coalesced row reads; the outputs go back the same way.  Pair variables
-// stage their lo parts through a second pair of tiles.
+// q) are staged 32 positions at a time through [32][33] tiles: every lane
+// copies position q+7+lane of each row with cp.async (no registers, no
+// wait), the next block's copies issued before the current block is
+// filtered (two tiles per plane).  Step t reads column t of its own row and
+// leaves its output there; the tile then goes back with coalesced row
+// writes.  Pair variables stage their lo parts through a second tile pair.
 // warps per block: 4 for single FP32 variables, 2 when the lo tiles exist
 template <int NP>
 constexpr int x_warps()
 {
     return NP ? 2 : 4;
+}
+
+__device__ __forceinline__ void cp_async4(float *dst, const float *src, int src_bytes)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(smem_addr(dst)),
+                 "l"(src), "r"(src_bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit()
+{
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+template <int N>
+__device__ __forceinline__ void cp_async_wait()
+{
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
 template <bool PAIR>
@@ -591,13 +612,26 @@ __device__ __forceinline__ void filter_x_rows(const float *__restrict__ sbase,
                                               float *__restrict__ obase, float *__restrict__ olbase,
                                               int fpitch, int n, int nrows, int lane, int a, int b,
                                               bool exact, bool first, bool last, int q0,
-                                              const FiltF &f, float (*ti)[33], float (*to)[33],
-                                              float (*til)[33], float (*tol)[33])
+                                              const FiltF &f, float (*ti)[32][33],
+                                              float (*til)[32][33])
 {
     const bool active = lane < nrows;
     const long long roff = (long long)(active ? lane : 0) * fpitch;
     const float *__restrict__ s = sbase + roff;
     const float *__restrict__ sl = PAIR ? slbase + roff : nullptr;
+    // copies of block qb (appended positions qb+7 ..) into tile set `buf`;
+    // positions past the row end are zero-filled (0 source bytes)
+    auto issue = [&](int buf, int qb) {
+        const int pos = qb + 7 + lane;
+        const int nb = pos < n ? 4 : 0;
+        const int pc = pos < n ? pos : 0;
+        for (int r = 0; r < nrows; r++) {
+            cp_async4(&ti[buf][r][lane], sbase + (long long)r * fpitch + pc, nb);
+            if (PAIR) cp_async4(&til[buf][r][lane], slbase + (long long)r * fpitch + pc, nb);
+        }
+        cp_async_commit();
+    };
+    if (q0 < b) issue(0, q0);
     float wh[13], wl[13];
 #pragma unroll
     for (int t = 0; t < 13; t++) {
@@ -618,21 +652,27 @@ __device__ __forceinline__ void filter_x_rows(const float *__restrict__ sbase,
     }
     // Steps q = q0 .. b-1 in blocks of 32: block B covers steps
     // [q0+32B, q0+32B+32), appends positions q+7, writes outputs at q.
+    int buf = 0;
     for (int qb = q0; qb < b; qb += 32) {
-        const int pin = qb + 7;  // first appended position of the block
-        for (int r = 0; r < nrows; r++) {
-            const int pos = pin + lane;
-            ti[r][lane] = (pos < n) ? sbase[(long long)r * fpitch + pos] : 0.f;
-            if (PAIR) til[r][lane] = (pos < n) ? slbase[(long long)r * fpitch + pos] : 0.f;
+        const bool more = qb + 32 < b;
+        if (more) {
+            issue(buf ^ 1, qb + 32);
+            cp_async_wait<1>();  // this block's copies have landed
+        } else {
+            cp_async_wait<0>();
         }
         __syncwarp();
         const int nstep = min(32, b - qb);
+        float(*tb)[33] = ti[buf];
+        float(*tbl)[33] = til[PAIR ? buf : 0];
         for (int t = 0; t < nstep; t++) {
             float vh, vl = 0.f;
             if (PAIR) pass2_p(wh, wl, f, vh, vl);
             else vh = pass2_f(wh, f);
-            to[lane][t] = vh;
-            if (PAIR) tol[lane][t] = vl;
+            const float nh = tb[lane][t];
+            const float nl = PAIR ? tbl[lane][t] : 0.f;
+            tb[lane][t] = vh;
+            if (PAIR) tbl[lane][t] = vl;
 #pragma unroll
             for (int u = 0; u < 5; u++) {
                 wh[u] = wh[u + 1];
@@ -645,19 +685,20 @@ __device__ __forceinline__ void filter_x_rows(const float *__restrict__ sbase,
                 wh[u] = wh[u + 1];
                 wl[u] = wl[u + 1];
             }
-            wh[12] = ti[lane][t];
-            wl[12] = PAIR ? til[lane][t] : 0.f;
+            wh[12] = nh;
+            wl[12] = nl;
         }
         __syncwarp();
         // write outputs q = qb .. qb+nstep-1 that this chunk owns (q >= a)
         for (int r = 0; r < nrows; r++) {
             const int qq = qb + lane;
             if (lane < nstep && qq >= a) {
-                obase[(long long)r * fpitch + qq] = to[r][lane];
-                if (PAIR) olbase[(long long)r * fpitch + qq] = tol[r][lane];
+                obase[(long long)r * fpitch + qq] = tb[r][lane];
+                if (PAIR) olbase[(long long)r * fpitch + qq] = tbl[r][lane];
             }
         }
         __syncwarp();
+        buf ^= 1;
     }
     if (last && active) {
         // w[0..11] = positions n-12 .. n-1 (pass 3)
@@ -680,8 +721,8 @@ __device__ __forceinline__ void split_filter_x_body(Dims d, int fpitch, const fl
 {
     constexpr int kXW = x_warps<NP>();
     constexpr int kXL = NP ? kXW : 1;  // lo tiles only when pairs exist
-    __shared__ float tin[kXW][32][33], tout[kXW][32][33];
-    __shared__ float tinl[kXL][32][33], toutl[kXL][32][33];
+    __shared__ float tin[kXW][2][32][33];
+    __shared__ float tinl[kXL][2][32][33];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int rows32 = (d.jmax + 31) / 32;
     const long long gw = (long long)blockIdx.x * kXW + wid;  // global warp
@@ -704,11 +745,11 @@ __device__ __forceinline__ void split_filter_x_body(Dims d, int fpitch, const fl
         filter_x_rows<true>(src + k * fplane + roff, src + (k + 3) * fplane + roff,
                             dst + k * fplane + roff, dst + (k + 3) * fplane + roff, fpitch, n,
                             nrows, lane, a, b, exact, c == 0, c == chunks - 1, q0, f, tin[wid],
-                            tout[wid], tinl[NP ? wid : 0], toutl[NP ? wid : 0]);
+                            tinl[NP ? wid : 0]);
     else
         filter_x_rows<false>(src + k * fplane + roff, nullptr, dst + k * fplane + roff, nullptr,
                              fpitch, n, nrows, lane, a, b, exact, c == 0, c == chunks - 1, q0, f,
-                             tin[wid], tout[wid], tinl[0], toutl[0]);
+                             tin[wid], tinl[0]);
 }
 
 // Register budgets measured best: the all-FP32 variant at one block per SM
