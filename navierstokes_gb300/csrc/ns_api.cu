@@ -7,6 +7,7 @@
 // LDDRK tables (rk.f90:27-46), the transport reference values
 // (coefficients.f90:71-80), the buffer arrays and the base flow.  One step
 // is captured once as a CUDA graph and replayed.
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -285,6 +286,10 @@ void free_all(ns_ctx *c)
             if (b) cudaFree(b);
     }
     if (c->step_exec) cudaGraphExecDestroy(c->step_exec);
+    if (c->tail_exec) cudaGraphExecDestroy(c->tail_exec);
+    for (cudaEvent_t ev : c->band_ev)
+        if (ev) cudaEventDestroy(ev);
+    if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     double *bufs[] = {c->U,    c->U2,   c->W,     c->dudm, c->dudn, c->aux,
                       c->Ubase, c->src, c->xcoef, c->ycoef, c->sigx, c->sigy,
                       c->rhob, c->psib, c->stage_sin, c->trtab, c->probe_buf, c->rec_buf,
@@ -934,27 +939,34 @@ int ns_get_state(ns_ctx *c, double *U, int layout)
     return check_kernel_err(c);
 }
 
-static int ensure_graph(ns_ctx *c)
+// Captures the launches `fn` makes into *exec (once).
+static int capture_graph(ns_ctx *c, cudaGraphExec_t *exec,
+                         cudaError_t (*fn)(ns_ctx *, cudaStream_t), const char *what)
 {
-    if (c->step_exec) return NS_OK;
+    if (*exec) return NS_OK;
     cudaStream_t cs;
     NS_CUDA(c, cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-        cudaError_t le = ns::launch_step(c, cs);
+        cudaError_t le = fn(c, cs);
         e = cudaStreamEndCapture(cs, &g);
         if (le != cudaSuccess) e = le;
     }
-    if (e == cudaSuccess) e = cudaGraphInstantiate(&c->step_exec, g, 0);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(exec, g, 0);
     if (g) cudaGraphDestroy(g);
     cudaStreamDestroy(cs);
     if (e != cudaSuccess) {
-        c->step_exec = nullptr;
+        *exec = nullptr;
         cudaGetLastError();
-        return cuda_err(c, e, "capture of the step graph");
+        return cuda_err(c, e, what);
     }
     return NS_OK;
+}
+
+static int ensure_graph(ns_ctx *c)
+{
+    return capture_graph(c, &c->step_exec, ns::launch_step, "capture of the step graph");
 }
 
 int ns_step(ns_ctx *c, int iter0, int nsteps)
@@ -993,6 +1005,58 @@ int ns_synchronize(ns_ctx *c)
     return check_kernel_err(c);
 }
 
+// FP64 ns_rk_euler on page-locked host memory.  The host array is copied
+// band by band (row bands, in U's own layout) by a copy engine into U2;
+// each band is converted to planes as it lands, and stage 0's k_prim and
+// k_first run on the bands already converted (k_first of band b once band
+// b+1 holds its 3-row halo), so the transfer overlaps that work.  The rest
+// of the step is a second captured graph; the result goes back to the host
+// array with one pass of the layout kernel.
+static int rk_euler_banded(ns_ctx *c, double *U, double *hv, int iter)
+{
+    const ns::Dims &d = c->d;
+    int rc = capture_graph(c, &c->tail_exec, ns::launch_step_tail, "capture of the step tail");
+    if (rc != NS_OK) return rc;
+    if (!c->copy_stream) {
+        NS_CUDA(c, cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+        for (cudaEvent_t &ev : c->band_ev)
+            NS_CUDA(c, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    }
+    constexpr int kMaxBands = 8;
+    const int nb = std::max(1, std::min(kMaxBands, d.jmax / 64));
+    const int rows = ((d.jmax + nb - 1) / nb + 7) / 8 * 8;
+    // the copies into U2 wait for earlier work on the context's stream
+    static_assert(sizeof(c->band_ev) / sizeof(c->band_ev[0]) > kMaxBands, "band events");
+    NS_CUDA(c, cudaEventRecord(c->band_ev[kMaxBands], c->stream));
+    NS_CUDA(c, cudaStreamWaitEvent(c->copy_stream, c->band_ev[kMaxBands], 0));
+    const size_t row_elems = (size_t)d.nk * d.imax;
+    int r0[kMaxBands], nr[kMaxBands], n = 0;
+    for (int j = 0; j < d.jmax; j += rows, n++) {
+        r0[n] = j;
+        nr[n] = std::min(rows, d.jmax - j);
+        NS_CUDA(c, cudaMemcpyAsync(c->U2 + row_elems * j, U + row_elems * j,
+                                   row_elems * nr[n] * sizeof(double), cudaMemcpyHostToDevice,
+                                   c->copy_stream));
+        NS_CUDA(c, cudaEventRecord(c->band_ev[n], c->copy_stream));
+    }
+    if (c->src) NS_CUDA(c, ns::launch_set_iter(c->d_iter, iter, c->stream));
+    for (int b = 0; b < n; b++) {
+        NS_CUDA(c, cudaStreamWaitEvent(c->stream, c->band_ev[b], 0));
+        ns::Dims db = d;
+        db.jmax = nr[b];
+        NS_CUDA(c, ns::launch_aos_to_soa(c->U2 + row_elems * r0[b], c->U + (size_t)r0[b] * d.pitch,
+                                         db, c->stream));
+        if (c->visc) NS_CUDA(c, ns::launch_rows(c, NS_KC_PRIM, r0[b], nr[b], c->stream));
+        if (b > 0) NS_CUDA(c, ns::launch_rows(c, NS_KC_FIRST, r0[b - 1], nr[b - 1], c->stream));
+    }
+    NS_CUDA(c, ns::launch_rows(c, NS_KC_FIRST, r0[n - 1], nr[n - 1], c->stream));
+    c->have_state = true;
+    NS_CUDA(c, cudaGraphLaunch(c->tail_exec, c->stream));
+    NS_CUDA(c, ns::launch_soa_to_aos(c->U, hv, d, c->stream));
+    NS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return check_kernel_err(c);
+}
+
 int ns_rk_euler(ns_ctx *c, double *U, double t, int iter, int nk)
 {
     (void)t;
@@ -1017,6 +1081,7 @@ int ns_rk_euler(ns_ctx *c, double *U, double t, int iter, int nk)
         return rc;
     }
     double *hv = static_cast<double *>(dev_view);
+    if (!c->split) return rk_euler_banded(c, U, hv, iter);
     NS_CUDA(c, ns::launch_aos_to_soa(hv, c->U, c->d, c->stream));
     if (c->split) NS_CUDA(c, ns::launch_split_from_full(c, c->U, c->stream));
     c->have_state = true;

@@ -194,6 +194,11 @@ struct ns_ctx {
     bool have_state = false;
     // captured one-step graph
     cudaGraphExec_t step_exec = nullptr;
+    // ns_rk_euler on page-locked host memory (FP64): the step without stage
+    // 0's k_prim/k_first, a copy stream and one event per row band
+    cudaGraphExec_t tail_exec = nullptr;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t band_ev[9] = {};
     cudaStream_t graph_stream = nullptr;
     int launches_per_step = 0;
     std::string err;
@@ -204,6 +209,11 @@ struct ns_ctx {
 namespace ns {
 constexpr int kMaxStepLaunches = 64;
 cudaError_t launch_step(ns_ctx *c, cudaStream_t s);
+// The step without stage 0's k_prim and k_first, and those two kernels over a
+// range of rows (FP64 contexts): ns_rk_euler runs them band by band as the
+// rows arrive from the host.
+cudaError_t launch_step_tail(ns_ctx *c, cudaStream_t s);
+cudaError_t launch_rows(ns_ctx *c, int cls, int row0, int rows, cudaStream_t s);
 cudaError_t launch_kernel(ns_ctx *c, int cls, int stage, cudaStream_t s);
 int step_sequence(const ns_ctx *c, int *cls, int *stage);
 cudaError_t launch_set_iter(int *d_iter, int iter, cudaStream_t s);

@@ -121,12 +121,14 @@ cudaError_t launch_transport_eval(const ns_ctx *c, const double *T, double *mu, 
 // ---------------------------------------------------------------------------
 // k_prim: T and 1/rho (rhs.f90:20), pointwise.
 // ---------------------------------------------------------------------------
+// Rows row0 .. row0+rows-1 (the whole grid in the step graph).
 __global__ void __launch_bounds__(256) k_prim(Dims d, const double *__restrict__ U,
-                                              double *__restrict__ aux, double gamma)
+                                              double *__restrict__ aux, double gamma, int row0,
+                                              int rows)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    if (i >= d.imax || j >= d.jmax) return;
+    const int j = row0 + blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= d.imax || j >= row0 + rows) return;
     const long long idx = (long long)j * d.pitch + i;
     const double rho = U[idx];
     const double p = U[3 * d.plane + idx];
@@ -141,13 +143,14 @@ __global__ void __launch_bounds__(256) k_prim(Dims d, const double *__restrict__
 // With TMA, one elected thread loads the block's halo tile of U (and of T)
 // into shared memory and the interior stencils read it there; the closure
 // points near the domain edges read global memory.  Both give identical bits.
+// Rows row0 .. row0+rows-1 (the whole grid in the step graph).
 template <bool VISC, int NK, bool TMA>
 __global__ void __launch_bounds__(256)
     k_first(const __grid_constant__ CUtensorMap umap, const __grid_constant__ CUtensorMap tmap,
             int *__restrict__ err, Dims d, const double *__restrict__ U,
             double *__restrict__ dudm, double *__restrict__ dudn, double *__restrict__ aux,
             const double *__restrict__ xcoef, const double *__restrict__ ycoef,
-            const double *__restrict__ trtab, Physics ph)
+            const double *__restrict__ trtab, Physics ph, int row0, int rows)
 {
     constexpr int TW = kFirstTileW, TH = kFirstTileH;
     __shared__ alignas(128) double su[TMA ? NK : 1][TMA ? TH : 1][TMA ? TW : 1];
@@ -155,7 +158,7 @@ __global__ void __launch_bounds__(256)
     __shared__ alignas(8) unsigned long long tbar;
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int i = blockIdx.x * kFirstBX + tx;
-    const int j = blockIdx.y * kFirstBY + ty;
+    const int j = row0 + blockIdx.y * kFirstBY + ty;
     if constexpr (TMA) {
         const bool lead = (tx == 0 && ty == 0);
         if (lead) mbar_init(&tbar, 1);
@@ -163,14 +166,15 @@ __global__ void __launch_bounds__(256)
         if (lead) {
             // boxes at (i0-4, j0-3): points outside the grid read as zero and
             // are never used (their neighbours take the closure branch)
-            const int x0 = blockIdx.x * kFirstBX - kFirstTileL, y0 = blockIdx.y * kFirstBY - 3;
+            const int x0 = blockIdx.x * kFirstBX - kFirstTileL;
+            const int y0 = row0 + blockIdx.y * kFirstBY - 3;
             mbar_expect_tx(&tbar, (unsigned)(sizeof(su) + (VISC ? sizeof(sT) : 0)));
             tma_load_3d(&su[0][0][0], &umap, x0, y0, 0, &tbar);
             if (VISC) tma_load_3d(&sT[0][0], &tmap, x0, y0, 0, &tbar);
         }
         if (!mbar_wait_bounded(&tbar, 0, err)) return;
     }
-    if (i >= d.imax || j >= d.jmax) return;
+    if (i >= d.imax || j >= row0 + rows) return;
     const long long idx = (long long)j * d.pitch + i;
     const long long P = d.plane, st = d.pitch;
     const double *cx = xcoef + kCoefStride * i;
@@ -742,6 +746,36 @@ static inline dim3 tile_grid(const Dims &d, dim3 blk)
     return dim3((d.imax + blk.x - 1) / blk.x, (d.jmax + blk.y - 1) / blk.y);
 }
 
+// k_prim or k_first over rows row0 .. row0+rows-1.
+template <bool VISC, int NK>
+static cudaError_t launch_rows_t(ns_ctx *c, int cls, int row0, int rows, cudaStream_t s)
+{
+    const Dims &d = c->d;
+    const dim3 blk(kFirstBX, kFirstBY);
+    const dim3 grd((d.imax + kFirstBX - 1) / kFirstBX, (rows + kFirstBY - 1) / kFirstBY);
+    if (cls == NS_KC_PRIM)
+        k_prim<<<grd, blk, 0, s>>>(d, c->U, c->aux, c->phys.gamma, row0, rows);
+    else if (c->fp64_maps)
+        k_first<VISC, NK, true><<<grd, blk, 0, s>>>(c->umap, c->tmap, c->d_err, d, c->U, c->dudm,
+                                                    c->dudn, c->aux, c->xcoef, c->ycoef,
+                                                    c->trtab, c->phys, row0, rows);
+    else
+        k_first<VISC, NK, false><<<grd, blk, 0, s>>>(c->umap, c->tmap, c->d_err, d, c->U,
+                                                     c->dudm, c->dudn, c->aux, c->xcoef,
+                                                     c->ycoef, c->trtab, c->phys, row0, rows);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_rows(ns_ctx *c, int cls, int row0, int rows, cudaStream_t s)
+{
+    if (c->split || (cls != NS_KC_PRIM && cls != NS_KC_FIRST)) return cudaErrorInvalidValue;
+    if (c->visc)
+        return c->d.nk == 5 ? launch_rows_t<true, 5>(c, cls, row0, rows, s)
+                            : launch_rows_t<true, 4>(c, cls, row0, rows, s);
+    return c->d.nk == 5 ? launch_rows_t<false, 5>(c, cls, row0, rows, s)
+                        : launch_rows_t<false, 4>(c, cls, row0, rows, s);
+}
+
 // One kernel of class `cls` (NS_KC_*) for `stage`.
 template <bool VISC, int NK>
 static cudaError_t launch_kernel_t(ns_ctx *c, int cls, int stage, cudaStream_t s)
@@ -751,18 +785,8 @@ static cudaError_t launch_kernel_t(ns_ctx *c, int cls, int stage, cudaStream_t s
     const dim3 grd = tile_grid(d, blk);
     switch (cls) {
     case NS_KC_PRIM:
-        k_prim<<<grd, blk, 0, s>>>(d, c->U, c->aux, c->phys.gamma);
-        break;
     case NS_KC_FIRST:
-        if (c->fp64_maps)
-            k_first<VISC, NK, true><<<grd, blk, 0, s>>>(c->umap, c->tmap, c->d_err, d, c->U,
-                                                        c->dudm, c->dudn, c->aux, c->xcoef,
-                                                        c->ycoef, c->trtab, c->phys);
-        else
-            k_first<VISC, NK, false><<<grd, blk, 0, s>>>(c->umap, c->tmap, c->d_err, d, c->U,
-                                                         c->dudm, c->dudn, c->aux, c->xcoef,
-                                                         c->ycoef, c->trtab, c->phys);
-        break;
+        return launch_rows_t<VISC, NK>(c, cls, 0, d.jmax, s);
     case NS_KC_UPDATE: {
         StageCoef sc{c->alpha[stage], c->beta[stage], stage};
         const bool src = c->src != nullptr;
@@ -857,6 +881,20 @@ int step_sequence(const ns_ctx *c, int *cls, int *stage)
         cls[n] = NS_KC_BC; stage[n++] = st;
     }
     return n;
+}
+
+// The step without stage 0's k_prim and k_first (the source phase kept):
+// the rest of the step once those have run over all rows.
+cudaError_t launch_step_tail(ns_ctx *c, cudaStream_t s)
+{
+    int cls[kMaxStepLaunches], stage[kMaxStepLaunches];
+    const int n = step_sequence(c, cls, stage);
+    for (int q = 0; q < n; q++) {
+        if (stage[q] == 0 && (cls[q] == NS_KC_PRIM || cls[q] == NS_KC_FIRST)) continue;
+        cudaError_t e = launch_kernel(c, cls[q], stage[q], s);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 cudaError_t launch_step(ns_ctx *c, cudaStream_t s)
