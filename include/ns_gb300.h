@@ -161,7 +161,10 @@ NS_API int ns_synchronize(ns_ctx *ctx);
 
 /* The drop-in for one call `call rk_euler(U,t,iter,nk)` (euler.f90:130,
  * rk.f90:12): host U in the reference layout U(nk,imax,jmax) is uploaded,
- * advanced one step and written back.  t is unused, as in the reference. */
+ * advanced one step and written back.  t is unused, as in the reference.
+ * When U is page-locked host memory, FP64 contexts copy it in row bands and
+ * start the step on the bands already copied; split contexts read and write
+ * it in place from the GPU.  Returns when U holds the new state. */
 NS_API int ns_rk_euler(ns_ctx *ctx, double *U, double t, int iter, int nk);
 
 /* Reads U(1..nk) at np points (1-based i, j) into out[np*nk] (point-major):
