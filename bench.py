@@ -383,10 +383,11 @@ def adjoint_study(args, local):
     source field (b = 32 cells) whose amplitude is the Keys-cubic
     interpolant of 16x16 controls ~ N(0, 1e-3) (seed 0), omega = 0.5, 2000
     steps; loss = sum over steps of p'^2 at 32 observers on a circle of
-    radius 150 cells.  Times the plain FP64 forward (ns_step), the
-    checkpointed forward with the loss (checkpoints every 100 steps) and the
-    reverse pass (segment recompute + stage adjoints), and checks the
-    control gradient at two controls against central differences h = 1e-7."""
+    radius 150 cells.  Times the plain FP64 forward (ns_step), the forward
+    with the loss (every stage input kept when it fits, --adjoint-k 0; else
+    checkpoints) and the reverse pass (stage derivatives or segments
+    recomputed, then the stage adjoints), and checks the control gradient at
+    two controls against central differences h = 1e-7."""
     import time
     from navierstokes_gb300 import Solver
     from navierstokes_gb300.adjoint import Adjoint, SourceProblem
@@ -411,6 +412,7 @@ def adjoint_study(args, local):
         t0 = time.perf_counter()
         loss = adj.forward()
         t_fwd = time.perf_counter() - t0
+        stored = adj.stored_bytes()
         t0 = time.perf_counter()
         gfield = adj.backward()
         t_bwd = time.perf_counter() - t0
@@ -432,7 +434,9 @@ def adjoint_study(args, local):
                 "backward_s": t_bwd, "backward_over_plain_forward": t_bwd / t_plain,
                 "gradient_cost_over_plain_forward": (t_fwd + t_bwd) / t_plain,
                 "plain_forward_value": c.points * pb.steps / t_plain / 1e6, "unit": UNIT,
-                "fd_check": fd, "grad_norm": float(np.linalg.norm(gc))})
+                "fd_check": fd, "grad_norm": float(np.linalg.norm(gc)),
+                "forward_storage": (f"every stage input kept: {stored / 1e9:.1f} GB" if stored
+                                    else f"checkpoints every {args.adjoint_k or 100} steps")})
     return out
 
 
@@ -699,7 +703,8 @@ def main():
     ap.add_argument("--cpu-workloads", action="store_true",
                     help="also time the C oracle on every workload (all cores, 1 core)")
     ap.add_argument("--adjoint-steps", type=int, default=2000)
-    ap.add_argument("--adjoint-k", type=int, default=100)
+    ap.add_argument("--adjoint-k", type=int, default=0,
+                    help="adjoint checkpoint interval; 0 keeps every stage input if it fits")
     ap.add_argument("--split-error-steps", type=lambda t: [int(x) for x in t.split(",")],
                     default=[100, 500, 1000])
     args = ap.parse_args()

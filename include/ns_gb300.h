@@ -274,8 +274,13 @@ NS_API int ns_batch_barrier_test(ns_batch *b, int extra, long long spin_limit);
  * p' = p - p_b interpolated bilinearly, with respect to the source field
  * S(i,j) of rk.f90:188-189 (s = sin(wf*(iter+c_k)*dt) * S).  The reverse pass
  * transposes ccpml, both filter sweeps, bufferxy, rk_steep, the pointwise
- * Jacobians of EULERNONLINEAR and the DRP stencils with their closures;
- * the forward state is checkpointed every checkpoint_every steps.
+ * Jacobians of EULERNONLINEAR and the DRP stencils with their closures.
+ * checkpoint_every >= 1: the forward state is checkpointed every
+ * checkpoint_every steps and the reverse pass recomputes each segment.
+ * checkpoint_every = 0: every stage's input state is kept (nsteps x 6 x 4
+ * planes) when that fits in three quarters of the free device memory, and
+ * the reverse pass recomputes only each stage's first derivatives;
+ * otherwise checkpoints every 100 steps.
  */
 typedef struct ns_adjoint ns_adjoint;
 NS_API int ns_adjoint_create(const ns_params *p, int nobs, const double *obs_x,
@@ -291,6 +296,8 @@ NS_API int ns_adjoint_forward(ns_adjoint *a, const double *U0, int layout, int i
 NS_API int ns_adjoint_backward(ns_adjoint *a, double *grad_field);
 /* The forward context (for its state and diagnostics). */
 NS_API int ns_adjoint_context(ns_adjoint *a, ns_ctx **ctx);
+/* Bytes of stage inputs the last forward pass kept (0: it checkpointed). */
+NS_API int ns_adjoint_stored_bytes(const ns_adjoint *a, int64_t *bytes);
 
 /*
  * The program around the step: euler.f90's time loop with its probes and

@@ -78,7 +78,9 @@ class SourceProblem:
 
 
 class Adjoint:
-    """ns_adjoint_* wrapper."""
+    """ns_adjoint_* wrapper.  checkpoint_every = 0 keeps every stage's input
+    state when device memory allows (the reverse pass then recomputes only
+    first derivatives), else checkpoints every 100 steps."""
 
     def __init__(self, problem: SourceProblem, checkpoint_every=100, device=0):
         self.lib = L.load()
@@ -121,6 +123,12 @@ class Adjoint:
                                             int(iter0), int(nsteps or self.problem.steps),
                                             C.byref(loss)))
         return loss.value
+
+    def stored_bytes(self) -> int:
+        """Bytes of stage inputs the last forward pass kept (0: checkpoints)."""
+        b = C.c_int64()
+        L.check(self.lib.ns_adjoint_stored_bytes(self._h, C.byref(b)))
+        return b.value
 
     def backward(self) -> np.ndarray:
         c = self.problem.case

@@ -51,6 +51,22 @@ __global__ void k_obs_loss(const double *U, Dims d, const Obs *obs, int nobs, do
     if (threadIdx.x == 0) *loss += acc;
 }
 
+// Copies the 4 state planes (n4 = 4*plane contiguous doubles) to slot
+// (*d_step)*6 + stage of the per-stage store; the step index is read on the
+// device, so one captured graph serves every step.
+__global__ void k_store_stage(const double *__restrict__ U, double *__restrict__ store,
+                              const int *__restrict__ d_step, int stage, long long n4)
+{
+    const long long off = ((long long)(*d_step) * 6 + stage) * n4;
+    const double2 *src = reinterpret_cast<const double2 *>(U);
+    double2 *dst = reinterpret_cast<double2 *>(store + off);
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n4 / 2;
+         e += (long long)gridDim.x * blockDim.x)
+        dst[e] = src[e];
+}
+
+__global__ void k_step_inc(int *d_step) { *d_step += 1; }
+
 // lam_p += dL/dp of sum_m p'_m^2 at U
 __global__ void k_obs_grad(const double *U, Dims d, const Obs *obs, int nobs, double pb,
                            double *lam)
@@ -401,6 +417,15 @@ struct ns_adjoint {
     double *chk = nullptr;     // checkpoints: nchk x 4 planes
     int nchk = 0;
     double *store = nullptr;   // segment: K steps x 6 stages x 12 planes (U, dU/dx, dU/dy)
+    // K = 0: every stage's input of every step kept (nsteps x 6 x 4 planes)
+    // when device memory allows; the reverse pass then recomputes only the
+    // first derivatives of each stage instead of the whole forward
+    double *stages = nullptr;
+    int stages_cap = 0;        // steps the stage store holds
+    int *d_step = nullptr;
+    cudaGraphExec_t fwd_exec = nullptr;  // one step with stage stores and the loss
+    bool stored_all = false;   // the last forward kept every stage input
+    int store_steps = 0;       // steps the segment store holds (0: one stage's scratch)
     double *endstate = nullptr;
     double *lam = nullptr, *lam2 = nullptr, *om = nullptr, *lx = nullptr, *ly = nullptr;
     double *gS = nullptr;
@@ -411,6 +436,9 @@ struct ns_adjoint {
 };
 
 namespace {
+
+// checkpoint interval when every-stage storage was asked for but does not fit
+constexpr int kDefaultCheckpoint = 100;
 
 int aerr(ns_adjoint *a, int code, const std::string &m)
 {
@@ -457,13 +485,14 @@ int forward_step(ns_adjoint *a, int iter, double *slot)
     return NS_OK;
 }
 
-int stage_adjoint(ns_adjoint *a, const double *slot, int stage, double sink)
+// The reverse of one stage: U, Um, Un are the stage's input state and its
+// first derivatives (4 planes each).
+int stage_adjoint(ns_adjoint *a, const double *U, const double *Um, const double *Un, int stage,
+                  double sink)
 {
     ns_ctx *c = a->fwd;
     const ns::Dims &d = c->d;
-    const size_t P = (size_t)d.plane;
     cudaStream_t s = c->stream;
-    const double *U = slot + (size_t)stage * 12 * P;
     ns::adj::k_bct_cols<<<(d.imax + 127) / 128, 128, 0, s>>>(a->lam, d);
     ns::adj::k_bct_rows<<<(d.jmax + 127) / 128, 128, 0, s>>>(a->lam, d);
     {
@@ -475,11 +504,85 @@ int stage_adjoint(ns_adjoint *a, const double *slot, int stage, double sink)
             d, a->lam2, a->lam, c->fx_chunks, c->warm, c->fx);
     }
     const dim3 blk(32, 8), grd((d.imax + 31) / 32, (d.jmax + 7) / 8);
-    ns::adj::k_point_t<<<grd, blk, 0, s>>>(d, a->lam, a->om, a->lx, a->ly, U, U + 4 * P, U + 8 * P,
+    ns::adj::k_point_t<<<grd, blk, 0, s>>>(d, a->lam, a->om, a->lx, a->ly, U, Um, Un,
                                            c->sigx, c->sigy, a->gS, c->phys.gamma, c->p.dt,
                                            c->alpha[stage], c->beta[stage], sink);
     ns::adj::k_deriv_t<<<grd, blk, 0, s>>>(d, a->lam, a->lx, a->ly, c->xcoef, c->ycoef);
     A_CUDA(a, cudaGetLastError());
+    return NS_OK;
+}
+
+// One forward step that copies every stage's input into the stage store,
+// then adds the step's loss term and advances the device step index.
+cudaError_t launch_forward_store(ns_adjoint *a, cudaStream_t s)
+{
+    ns_ctx *c = a->fwd;
+    const long long n4 = 4LL * c->d.plane;
+    int cls[ns::kMaxStepLaunches], stg[ns::kMaxStepLaunches];
+    const int n = ns::step_sequence(c, cls, stg);
+    const unsigned nb = (unsigned)std::min<long long>((n4 / 2 + 255) / 256, 4LL * 152);
+    for (int q = 0; q < n; q++) {
+        if (cls[q] == NS_KC_FIRST)
+            ns::adj::k_store_stage<<<nb, 256, 0, s>>>(c->U, a->stages, a->d_step, stg[q], n4);
+        cudaError_t e = ns::launch_kernel(c, cls[q], stg[q], s);
+        if (e != cudaSuccess) return e;
+    }
+    ns::adj::k_obs_loss<<<1, 32, 0, s>>>(c->U, c->d, a->obs, a->nobs, a->pb, a->loss);
+    ns::adj::k_step_inc<<<1, 1, 0, s>>>(a->d_step);
+    return cudaGetLastError();
+}
+
+// The stage store for nsteps steps, when it fits in device memory with a
+// quarter of the free memory to spare; false: use checkpoints instead.
+bool ensure_stages(ns_adjoint *a, int nsteps)
+{
+    if (a->stages && a->stages_cap >= nsteps) return true;
+    ns_ctx *c = a->fwd;
+    const size_t bytes = (size_t)nsteps * 6 * 4 * (size_t)c->d.plane * sizeof(double);
+    if (a->fwd_exec) {
+        cudaGraphExecDestroy(a->fwd_exec);  // it holds the old store's address
+        a->fwd_exec = nullptr;
+    }
+    if (a->stages) cudaFree(a->stages);
+    a->stages = nullptr;
+    a->stages_cap = 0;
+    size_t freeb = 0, total = 0;
+    if (cudaMemGetInfo(&freeb, &total) != cudaSuccess || bytes > freeb / 4 * 3) {
+        cudaGetLastError();
+        return false;
+    }
+    if (cudaMalloc(&a->stages, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        a->stages = nullptr;
+        return false;
+    }
+    a->stages_cap = nsteps;
+    return true;
+}
+
+int ensure_forward_graph(ns_adjoint *a)
+{
+    if (a->fwd_exec) return NS_OK;
+    ns_ctx *c = a->fwd;
+    cudaStream_t cs;
+    A_CUDA(a, cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        const cudaError_t le = launch_forward_store(a, cs);
+        e = cudaStreamEndCapture(cs, &g);
+        if (le != cudaSuccess) e = le;
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&a->fwd_exec, g, 0);
+    if (g) cudaGraphDestroy(g);
+    cudaStreamDestroy(cs);
+    (void)c;
+    if (e != cudaSuccess) {
+        a->fwd_exec = nullptr;
+        cudaGetLastError();
+        return aerr(a, NS_ERR_CUDA, std::string("capture of the adjoint forward step: ") +
+                                        cudaGetErrorString(e));
+    }
     return NS_OK;
 }
 
@@ -490,7 +593,7 @@ extern "C" {
 int ns_adjoint_create(const ns_params *p, int nobs, const double *obs_x, const double *obs_y,
                       int checkpoint_every, ns_adjoint **out)
 {
-    if (!out || !p || nobs < 1 || !obs_x || !obs_y || checkpoint_every < 1)
+    if (!out || !p || nobs < 1 || !obs_x || !obs_y || checkpoint_every < 0)
         return aerr(nullptr, NS_ERR_PARAM, "ns_adjoint_create: bad argument");
     *out = nullptr;
     if (!p->inviscid || p->nk != 4 || p->precision != NS_PREC_FP64 ||
@@ -529,7 +632,10 @@ int ns_adjoint_create(const ns_params *p, int nobs, const double *obs_x, const d
     const size_t P = (size_t)c->d.plane;
     cudaError_t e = cudaMalloc(&a->obs, nobs * sizeof(ns::adj::Obs));
     if (e == cudaSuccess) e = cudaMalloc(&a->loss, sizeof(double));
-    if (e == cudaSuccess) e = cudaMalloc(&a->store, (size_t)a->K * 6 * 12 * P * sizeof(double));
+    a->store_steps = a->K;
+    const size_t store_planes = a->K ? (size_t)a->K * 6 * 12 : 12;
+    if (e == cudaSuccess) e = cudaMalloc(&a->store, store_planes * P * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&a->d_step, sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&a->endstate, 4 * P * sizeof(double));
     double **bufs[] = {&a->lam, &a->lam2, &a->om, &a->lx, &a->ly};
     for (double **b : bufs)
@@ -555,8 +661,9 @@ void ns_adjoint_destroy(ns_adjoint *a)
         a->fwd->dudm = a->dudm0;
         a->fwd->dudn = a->dudn0;
     }
+    if (a->fwd_exec) cudaGraphExecDestroy(a->fwd_exec);
     void *ps[] = {a->obs, a->loss, a->chk, a->store, a->endstate, a->lam, a->lam2, a->om,
-                  a->lx, a->ly, a->gS};
+                  a->lx, a->ly, a->gS, a->stages, a->d_step};
     for (void *p : ps)
         if (p) cudaFree(p);
     if (a->fwd) ns_destroy(a->fwd);
@@ -586,18 +693,43 @@ int ns_adjoint_forward(ns_adjoint *a, const double *U0, int layout, int iter0, i
     const size_t P = (size_t)c->d.plane;
     int rc = ns_set_state(c, U0, layout);
     if (rc != NS_OK) return rc;
-    const int nchk = (nsteps + a->K - 1) / a->K;
+    cudaStream_t s = c->stream;
+    a->stored_all = (a->K == 0) && ensure_stages(a, nsteps);
+    if (a->stored_all) {
+        if ((rc = ensure_forward_graph(a)) != NS_OK) return rc;
+        A_CUDA(a, cudaMemsetAsync(a->loss, 0, sizeof(double), s));
+        A_CUDA(a, cudaMemsetAsync(a->d_step, 0, sizeof(int), s));
+        A_CUDA(a, ns::launch_set_iter(c->d_iter, iter0, s));
+        for (int n = 0; n < nsteps; n++) A_CUDA(a, cudaGraphLaunch(a->fwd_exec, s));
+        A_CUDA(a, cudaMemcpyAsync(a->endstate, c->U, 4 * P * sizeof(double),
+                                  cudaMemcpyDeviceToDevice, s));
+        A_CUDA(a, cudaMemcpyAsync(loss, a->loss, sizeof(double), cudaMemcpyDeviceToHost, s));
+        if ((rc = ns_synchronize(c)) != NS_OK) return aerr(a, rc, ns_last_error(c));
+        a->nsteps = nsteps;
+        a->iter0 = iter0;
+        a->forward_done = true;
+        return NS_OK;
+    }
+    const int K = a->K ? a->K : kDefaultCheckpoint;
+    if (a->store_steps < K) {
+        // every-stage storage did not fit: segments of K steps
+        if (a->store) cudaFree(a->store);
+        a->store = nullptr;
+        a->store_steps = 0;
+        A_CUDA(a, cudaMalloc(&a->store, (size_t)K * 6 * 12 * P * sizeof(double)));
+        a->store_steps = K;
+    }
+    const int nchk = (nsteps + K - 1) / K;
     if (nchk > a->nchk) {
         if (a->chk) cudaFree(a->chk);
         a->chk = nullptr;
         A_CUDA(a, cudaMalloc(&a->chk, (size_t)nchk * 4 * P * sizeof(double)));
         a->nchk = nchk;
     }
-    cudaStream_t s = c->stream;
     A_CUDA(a, cudaMemsetAsync(a->loss, 0, sizeof(double), s));
     for (int n = 0; n < nsteps; n++) {
-        if (n % a->K == 0)
-            A_CUDA(a, cudaMemcpyAsync(a->chk + (size_t)(n / a->K) * 4 * P, c->U, 4 * P * sizeof(double),
+        if (n % K == 0)
+            A_CUDA(a, cudaMemcpyAsync(a->chk + (size_t)(n / K) * 4 * P, c->U, 4 * P * sizeof(double),
                                       cudaMemcpyDeviceToDevice, s));
         rc = ns_step(c, iter0 + n, 1);
         if (rc != NS_OK) return rc;
@@ -623,10 +755,39 @@ int ns_adjoint_backward(ns_adjoint *a, double *grad_field)
     cudaStream_t s = c->stream;
     A_CUDA(a, cudaMemsetAsync(a->lam, 0, 4 * P * sizeof(double), s));
     A_CUDA(a, cudaMemsetAsync(a->gS, 0, P * sizeof(double), s));
-    const int nseg = (a->nsteps + a->K - 1) / a->K;
     int rc;
+    if (a->stored_all) {
+        // every stage input is stored: per stage, only its first derivatives
+        // are recomputed (k_first on a copy in the context's U, into the
+        // scratch slot), then the stage is reversed
+        double *Um = a->store + 4 * P, *Un = a->store + 8 * P;
+        for (int n = a->nsteps - 1; n >= 0; n--) {
+            const double *Unext = (n == a->nsteps - 1)
+                                      ? a->endstate
+                                      : a->stages + (size_t)(n + 1) * 6 * 4 * P;
+            ns::adj::k_obs_grad<<<(a->nobs + 63) / 64, 64, 0, s>>>(Unext, d, a->obs, a->nobs,
+                                                                  a->pb, a->lam);
+            A_CUDA(a, cudaMemsetAsync(a->om, 0, 4 * P * sizeof(double), s));
+            double sn[6];
+            stage_sines(c, a->iter0 + n, sn);
+            for (int st = 5; st >= 0; st--) {
+                const double *U = a->stages + ((size_t)n * 6 + st) * 4 * P;
+                A_CUDA(a, cudaMemcpyAsync(c->U, U, 4 * P * sizeof(double),
+                                          cudaMemcpyDeviceToDevice, s));
+                c->dudm = Um;
+                c->dudn = Un;
+                const cudaError_t e = ns::launch_kernel(c, NS_KC_FIRST, st, s);
+                c->dudm = a->dudm0;
+                c->dudn = a->dudn0;
+                A_CUDA(a, e);
+                if ((rc = stage_adjoint(a, U, Um, Un, st, sn[st])) != NS_OK) return rc;
+            }
+        }
+    }
+    const int K = a->K ? a->K : kDefaultCheckpoint;
+    const int nseg = a->stored_all ? 0 : (a->nsteps + K - 1) / K;
     for (int sg = nseg - 1; sg >= 0; sg--) {
-        const int n0 = sg * a->K, n1 = std::min(a->nsteps, n0 + a->K);
+        const int n0 = sg * K, n1 = std::min(a->nsteps, n0 + K);
         // recompute the segment, keeping every stage's input and derivatives
         A_CUDA(a, cudaMemcpyAsync(c->U, a->chk + (size_t)sg * 4 * P, 4 * P * sizeof(double),
                                   cudaMemcpyDeviceToDevice, s));
@@ -641,8 +802,11 @@ int ns_adjoint_backward(ns_adjoint *a, double *grad_field)
             double sn[6];
             stage_sines(c, a->iter0 + n, sn);
             const double *slot = a->store + (size_t)(n - n0) * 6 * 12 * P;
-            for (int st = 5; st >= 0; st--)
-                if ((rc = stage_adjoint(a, slot, st, sn[st])) != NS_OK) return rc;
+            for (int st = 5; st >= 0; st--) {
+                const double *U = slot + (size_t)st * 12 * P;
+                if ((rc = stage_adjoint(a, U, U + 4 * P, U + 8 * P, st, sn[st])) != NS_OK)
+                    return rc;
+            }
         }
     }
     const size_t row = (size_t)d.imax * sizeof(double);
@@ -651,6 +815,14 @@ int ns_adjoint_backward(ns_adjoint *a, double *grad_field)
     if ((rc = ns_synchronize(c)) != NS_OK) return aerr(a, rc, ns_last_error(c));
     // leave the context's state at the forward end state
     A_CUDA(a, cudaMemcpy(c->U, a->endstate, 4 * P * sizeof(double), cudaMemcpyDeviceToDevice));
+    return NS_OK;
+}
+
+int ns_adjoint_stored_bytes(const ns_adjoint *a, int64_t *bytes)
+{
+    if (!a || !bytes) return aerr(nullptr, NS_ERR_PARAM, "ns_adjoint_stored_bytes: NULL argument");
+    *bytes = a->stored_all ? (int64_t)a->nsteps * 6 * 4 * a->fwd->d.plane * (int64_t)sizeof(double)
+                           : 0;
     return NS_OK;
 }
 

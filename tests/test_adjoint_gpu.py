@@ -33,14 +33,16 @@ def rel_field_err(g, ref):
     return float(np.abs(g - ref).max() / np.abs(ref).max())
 
 
-@pytest.mark.parametrize("K", [1, 2, 5])
+@pytest.mark.parametrize("K", [0, 1, 2, 5])
 def test_adjoint_matches_torch_autograd(nslib, oracle_mod, K):
+    # K = 0: every stage input kept, only first derivatives recomputed
     pb = small_problem(steps=5)
     S = pb.case.src_field
     L_ref, g_ref, _ = torch_ref.loss_and_grad(pb.case, S, pb.obs_x, pb.obs_y, 5)
     with Adjoint(pb, checkpoint_every=K) as adj:
         adj.set_field(S)
         L = adj.forward(5)
+        assert (adj.stored_bytes() > 0) == (K == 0)
         g = adj.backward()
     assert abs(L - L_ref) <= L_RTOL * abs(L_ref), (L, L_ref)
     err = rel_field_err(g, g_ref)
