@@ -176,29 +176,19 @@ __device__ __forceinline__ void shift13_down(double *w, double next)
     w[0] = next;
 }
 
-template <bool ALONG_Y>
-__global__ void __launch_bounds__(128)
-    k_filter_t(Dims d, const double *__restrict__ in, double *__restrict__ out, int chunks,
-               int warm, FilterCoef fc)
+// Pass-2 positions [a, b) of one line, transposed: b == n-6 starts exactly
+// with pass 3^T at the top, a later end runs `warm` points of history
+// first (or starts exactly when that reaches the top); a == 6 ends with
+// pass 1^T.  Writes positions a+6 .. b+5 (and 0..11 when a == 6, the top
+// when b == n-6).
+__device__ __forceinline__ void filter_piece_t(const double *__restrict__ s, double *__restrict__ o,
+                                               long long st, int n, int a, int b, int warm,
+                                               const FilterCoef &fc)
 {
-    const int nlines = ALONG_Y ? d.imax : d.jmax;
-    const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid >= (long long)nlines * 4 * chunks) return;
-    const int line = (int)(gid % nlines);
-    const int rest = (int)(gid / nlines);
-    const int k = rest % 4, c = rest / 4;
-    const int n = ALONG_Y ? d.jmax : d.imax;
-    const long long st = ALONG_Y ? d.pitch : 1;
-    const long long base = (long long)k * d.plane + (ALONG_Y ? line : (long long)line * d.pitch);
-    const double *__restrict__ s = in + base;
-    double *__restrict__ o = out + base;
-    const int len2 = n - 12;
-    const int a = 6 + (int)(((long long)c * len2) / chunks);
-    const int b = 6 + (int)(((long long)(c + 1) * len2) / chunks);
     double w[13];
     int q;
     const int qtop = n - 7;
-    if (c == chunks - 1 || warm < 0 || b - 1 + warm >= qtop) {
+    if (b == n - 6 || warm < 0 || b - 1 + warm >= qtop) {
         // exact start at the top: pass 3^T on positions n-12..n-1
         double L[12];
 #pragma unroll
@@ -247,7 +237,7 @@ __global__ void __launch_bounds__(128)
         if (q < b) o[(long long)(q + 6) * st] = w[12];
         shift13_down(w, (q - 7 >= 0) ? s[(long long)(q - 7) * st] : 0.0);
     }
-    if (c == 0) {
+    if (a == 6) {
         // window now holds positions -1..11 in w[0..12]: pass 1^T, q = 6..1
 #pragma unroll
         for (int qq = 6; qq >= 1; qq--) {
@@ -259,6 +249,40 @@ __global__ void __launch_bounds__(128)
         }
 #pragma unroll
         for (int p = 0; p < 12; p++) o[(long long)p * st] = w[p + 1];
+    }
+}
+
+// The transposed sweep dealt out like the forward one (k_filter): warp-lines
+// of 32 adjacent lines, their pass-2 positions laid end to end and cut into
+// equal segments, one per warp.
+template <bool ALONG_Y>
+__global__ void __launch_bounds__(128)
+    k_filter_t(Dims d, const double *__restrict__ in, double *__restrict__ out, long long seg,
+               int warm, FilterCoef fc)
+{
+    const int lane = threadIdx.x & 31;
+    const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nlines = ALONG_Y ? d.imax : d.jmax;
+    const int gpk = (nlines + 31) >> 5;
+    const int n = ALONG_Y ? d.jmax : d.imax;
+    const int len2 = n - 12;
+    const long long total = (long long)gpk * 4 * len2;
+    const long long s0 = wid * seg;
+    const long long s1 = s0 + seg < total ? s0 + seg : total;
+    const long long st = ALONG_Y ? d.pitch : 1;
+    for (long long sp = s0; sp < s1;) {
+        const long long g = sp / len2;
+        const long long gend = (g + 1) * len2;
+        const long long e = s1 < gend ? s1 : gend;
+        const int k = (int)(g / gpk);
+        const int line = (int)(g % gpk) * 32 + lane;
+        if (line < nlines) {
+            const long long base =
+                (long long)k * d.plane + (ALONG_Y ? line : (long long)line * d.pitch);
+            filter_piece_t(in + base, out + base, st, n, 6 + (int)(sp - g * len2),
+                           6 + (int)(e - g * len2), warm, fc);
+        }
+        sp = e;
     }
 }
 
@@ -496,12 +520,12 @@ int stage_adjoint(ns_adjoint *a, const double *U, const double *Um, const double
     ns::adj::k_bct_cols<<<(d.imax + 127) / 128, 128, 0, s>>>(a->lam, d);
     ns::adj::k_bct_rows<<<(d.jmax + 127) / 128, 128, 0, s>>>(a->lam, d);
     {
-        const long long ty = (long long)d.imax * 4 * c->fy_chunks;
-        ns::adj::k_filter_t<true><<<(unsigned)((ty + 127) / 128), 128, 0, s>>>(
-            d, a->lam, a->lam2, c->fy_chunks, c->warm, c->fy);
-        const long long tx = (long long)d.jmax * 4 * c->fx_chunks;
-        ns::adj::k_filter_t<false><<<(unsigned)((tx + 127) / 128), 128, 0, s>>>(
-            d, a->lam2, a->lam, c->fx_chunks, c->warm, c->fx);
+        long long seg;
+        unsigned nb;
+        ns::filter_shape(d.imax, d.jmax, 4, c->warm, c->nsm, ns::kFilterWarpsPerSmsp, seg, nb);
+        ns::adj::k_filter_t<true><<<nb, 128, 0, s>>>(d, a->lam, a->lam2, seg, c->warm, c->fy);
+        ns::filter_shape(d.jmax, d.imax, 4, c->warm, c->nsm, ns::kFilterWarpsPerSmsp, seg, nb);
+        ns::adj::k_filter_t<false><<<nb, 128, 0, s>>>(d, a->lam2, a->lam, seg, c->warm, c->fx);
     }
     const dim3 blk(32, 8), grd((d.imax + 31) / 32, (d.jmax + 7) / 8);
     ns::adj::k_point_t<<<grd, blk, 0, s>>>(d, a->lam, a->om, a->lx, a->ly, U, Um, Un,

@@ -226,32 +226,6 @@ int choose_chunks(int nlines_total, int n, int warm, int target_threads)
     return c;
 }
 
-// Chunks per line of the FP64 filters.  They are bound by the FP64 pipe of
-// each SM sub-partition, which one resident warp keeps busy (a DFMA warp
-// instruction occupies it for ~67 cycles, longer than the prefetched loads'
-// latency), so the time of a launch is about (warps on the busiest
-// sub-partition) x (points per thread).  Blocks of 128 threads put one warp
-// on each sub-partition of an SM; a chunk after the first also filters
-// `warm` points of warm-up.  Picks the count with the least such time.
-int choose_chunks_fp64(int nlines_total, int n, int warm, int nsm)
-{
-    if (warm < 0) return 1;
-    const int len2 = n - 12;
-    const int maxc = std::max(1, len2 / (warm + 6));
-    int best = 1;
-    long long best_cost = -1;
-    for (int c = 1; c <= maxc; c++) {
-        const long long blocks = ((long long)nlines_total * c + 127) / 128;
-        const long long per_smsp = (blocks + nsm - 1) / nsm;
-        const long long cost = per_smsp * ((len2 + c - 1) / c + (c > 1 ? warm : 0));
-        if (best_cost < 0 || cost < best_cost) {
-            best_cost = cost;
-            best = c;
-        }
-    }
-    return best;
-}
-
 template <class T>
 int dalloc(ns_ctx *c, T **p, size_t count);
 
@@ -867,8 +841,6 @@ constants:
         int nsm = 152;
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->dev);
         c->nsm = nsm;
-        c->fx_chunks = choose_chunks_fp64(d.jmax * d.nk, d.imax, c->warm, nsm);
-        c->fy_chunks = choose_chunks_fp64(d.imax * d.nk, d.jmax, c->warm, nsm);
         if (c->split) {
             // FP32 filters are bound by memory: aim at 32 resident warps per SM
             ns::SplitState &sp = c->sp;

@@ -186,7 +186,6 @@ struct ns_ctx {
     ns::FilterCoef fx, fy;
     double ct[6], alpha[6], beta[6];
     int warm = 0;       // filter warm-up length (-1: serial sweeps)
-    int fx_chunks = 1, fy_chunks = 1;  // chunks per line of the adjoint's filter transposes
     int nsm = 152;      // multiprocessors of the device
     bool visc = false;
     bool split = false;
@@ -214,6 +213,10 @@ cudaError_t launch_step(ns_ctx *c, cudaStream_t s);
 // rows arrive from the host.
 cudaError_t launch_step_tail(ns_ctx *c, cudaStream_t s);
 cudaError_t launch_rows(ns_ctx *c, int cls, int row0, int rows, cudaStream_t s);
+// Launch shape of the segmented filter sweeps (ns_kernels.cu): `seg`
+// pass-2 positions per warp, `blocks` blocks of 128 threads.
+void filter_shape(int nlines, int n, int nk, int warm, int nsm, int kw, long long &seg,
+                  unsigned &blocks);
 cudaError_t launch_kernel(ns_ctx *c, int cls, int stage, cudaStream_t s);
 int step_sequence(const ns_ctx *c, int *cls, int *stage);
 cudaError_t launch_set_iter(int *d_iter, int iter, cudaStream_t s);

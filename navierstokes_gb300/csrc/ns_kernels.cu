@@ -573,8 +573,8 @@ __global__ void __launch_bounds__(128)
 // warp-lines per warp when the warm-up is unbounded (warm < 0).  A warp
 // count just above a multiple of the sub-partitions would leave most of them
 // waiting for the few that run two warps, so the count is a multiple.
-static void filter_shape(int nlines, int n, int nk, int warm, int nsm, int kw, long long &seg,
-                         unsigned &blocks)
+void filter_shape(int nlines, int n, int nk, int warm, int nsm, int kw, long long &seg,
+                  unsigned &blocks)
 {
     const long long gtot = (long long)nk * ((nlines + 31) / 32);
     const int len2 = n - 12;
