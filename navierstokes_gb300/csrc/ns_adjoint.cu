@@ -587,7 +587,6 @@ bool ensure_stages(ns_adjoint *a, int nsteps)
 int ensure_forward_graph(ns_adjoint *a)
 {
     if (a->fwd_exec) return NS_OK;
-    ns_ctx *c = a->fwd;
     cudaStream_t cs;
     A_CUDA(a, cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
     cudaGraph_t g = nullptr;
@@ -600,7 +599,6 @@ int ensure_forward_graph(ns_adjoint *a)
     if (e == cudaSuccess) e = cudaGraphInstantiate(&a->fwd_exec, g, 0);
     if (g) cudaGraphDestroy(g);
     cudaStreamDestroy(cs);
-    (void)c;
     if (e != cudaSuccess) {
         a->fwd_exec = nullptr;
         cudaGetLastError();
