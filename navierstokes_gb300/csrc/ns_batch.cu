@@ -161,17 +161,49 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
 
 // The state buffers are written by other phases of the same launch, so they
 // are read through plain (coherent) loads: no __restrict__ / read-only path.
-template <typename T, int TY>
-__device__ void stage_tile(const Args &a, int st, int4 item, const T *qin, T *qout,
-                           unsigned char *smem)
+template <int TY>
+constexpr int tile_sw()
 {
-    constexpr int SW = kTX + 2 * kH, SH = TY + 2 * kH;
-    T(*sq)[SH][SW] = reinterpret_cast<T(*)[SH][SW]>(smem);
+    return kTX + 2 * kH;
+}
+template <int TY>
+constexpr int tile_sh()
+{
+    return TY + 2 * kH;
+}
+
+__device__ __forceinline__ unsigned smem_u32(const void *p)
+{
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+
+// One element global -> shared without registers; 0 source bytes fill zeros.
+template <typename T>
+__device__ __forceinline__ void cp_async_elem(T *dst, const T *src, bool ok)
+{
+    const int nb = ok ? (int)sizeof(T) : 0;
+    if constexpr (sizeof(T) == 8)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(smem_u32(dst)), "l"(src),
+                     "r"(nb)
+                     : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(smem_u32(dst)), "l"(src),
+                     "r"(nb)
+                     : "memory");
+}
+
+// Copies of the halo tile of `item` (4 planes, SH x SW) into sq, issued by
+// the whole block and committed as one group; points outside the instance
+// are zero.
+template <typename T, int TY>
+__device__ void tile_issue(const Args &a, int4 item, const T *qin, T *sqbuf)
+{
+    constexpr int SW = tile_sw<TY>(), SH = tile_sh<TY>();
+    T(*sq)[SH][SW] = reinterpret_cast<T(*)[SH][SW]>(sqbuf);
     const Inst in = a.inst[item.x];
     const int i0 = item.y, j0 = item.z;
     const long long plane = (long long)in.pitch * in.jmax;
     const T *q = qin + in.q_off;
-    T *qo = qout + in.q_off;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     for (int r = ty; r < SH; r += kWarps) {
         const int gj = j0 - kH + r;
@@ -179,12 +211,33 @@ __device__ void stage_tile(const Args &a, int st, int4 item, const T *qin, T *qo
         for (int cc = tx; cc < SW; cc += kTX) {
             const int gi = i0 - kH + cc;
             const bool ok = rowok && gi >= 0 && gi < in.imax;
-            const long long g = (long long)gj * in.pitch + gi;
+            const long long g = ok ? (long long)gj * in.pitch + gi : 0;
 #pragma unroll
-            for (int k = 0; k < 4; k++) sq[k][r][cc] = ok ? q[k * plane + g] : T(0);
+            for (int k = 0; k < 4; k++) cp_async_elem(&sq[k][r][cc], q + k * plane + g, ok);
         }
     }
-    __syncthreads();
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+template <int N>
+__device__ __forceinline__ void tile_wait()
+{
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// One tile of phase A from its staged halo tile (tile_issue, completed).
+template <typename T, int TY>
+__device__ void stage_tile(const Args &a, int st, int4 item, const T *qin, T *qout,
+                           const T *sqbuf)
+{
+    constexpr int SW = tile_sw<TY>(), SH = tile_sh<TY>();
+    const T(*sq)[SH][SW] = reinterpret_cast<const T(*)[SH][SW]>(sqbuf);
+    const Inst in = a.inst[item.x];
+    const int i0 = item.y, j0 = item.z;
+    const long long plane = (long long)in.pitch * in.jmax;
+    const T *q = qin + in.q_off;
+    T *qo = qout + in.q_off;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     const int i = i0 + tx;
     if (i < in.imax) {
         const T *cxp = tab<T>(a.xc) + (long long)kCoefStride * (in.x_off + i);
@@ -311,7 +364,6 @@ __device__ void stage_tile(const Args &a, int st, int4 item, const T *qin, T *qo
             for (int k = 0; k < 4; k++) qo[k * plane + idx] = qv[k];
         }
     }
-    __syncthreads();  // the tile buffer is reused by the next item
 }
 
 // ---------------------------------------------------------------------------
@@ -598,8 +650,27 @@ __global__ void __launch_bounds__(256) k_batch_step(Args a)
     for (int st = 0; st < 6; st++) {
         T *qa = reinterpret_cast<T *>((st & 1) ? a.q1 : a.q0);
         T *qb = reinterpret_cast<T *>((st & 1) ? a.q0 : a.q1);
-        for (int it = blockIdx.x; it < a.ntiles; it += gridDim.x)
-            stage_tile<T, TY>(a, st, a.tiles[it], qa, qb, smem);
+        {
+            // two tile buffers: the next item's copies are in flight while
+            // the current item is computed
+            constexpr size_t kTile = 4 * (size_t)tile_sh<TY>() * tile_sw<TY>();
+            T *buf[2] = {reinterpret_cast<T *>(smem), reinterpret_cast<T *>(smem) + kTile};
+            int b = 0;
+            if ((int)blockIdx.x < a.ntiles) tile_issue<T, TY>(a, a.tiles[blockIdx.x], qa, buf[0]);
+            for (int it = blockIdx.x; it < a.ntiles; it += gridDim.x) {
+                const int nx = it + (int)gridDim.x;
+                if (nx < a.ntiles) {
+                    tile_issue<T, TY>(a, a.tiles[nx], qa, buf[b ^ 1]);
+                    tile_wait<1>();
+                } else {
+                    tile_wait<0>();
+                }
+                __syncthreads();
+                stage_tile<T, TY>(a, st, a.tiles[it], qa, qb, buf[b]);
+                __syncthreads();  // buf[b] is refilled two items on
+                b ^= 1;
+            }
+        }
         if (!grid_barrier(a)) return;
         for_items(a.work + 2 * st, a.nfx,
                   [&](int wi) { fx_item<T, PW>(a, a.fx[wi], qb, qa, ti, to); });
@@ -888,7 +959,7 @@ size_t smem_for(int precision, int ty)
 {
     const size_t es = precision == NS_PREC_SPLIT32 ? 4 : 8;
     const int pw = precision == NS_PREC_SPLIT32 ? 32 : 16;
-    const size_t tile = 4 * (size_t)(ty + 6) * 38 * es;
+    const size_t tile = 2 * 4 * (size_t)(ty + 6) * 38 * es;  // two tile buffers
     const size_t fx = (size_t)ns::batch::kWarps * 2 * 32 * (pw + 1) * es;
     return std::max(tile, fx);
 }
