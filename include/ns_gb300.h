@@ -236,6 +236,13 @@ NS_API int ns_math_eval(int fn, const double *x, double *y, int n, int device);
  * inviscid context. */
 NS_API int ns_transport_eval(ns_ctx *ctx, const double *T, double *mu, double *k, int n);
 
+/* Library diagnostic, no counterpart in the reference: runs one block whose
+ * mbarrier expects bytes that no copy delivers, with the bounded wait of the
+ * TMA tile loads limited to spin_limit polls (1 .. 2^16).  Returns
+ * NS_ERR_TIMEOUT when the wait ran out and reported it, as the stage
+ * kernels do (their limit is 2^24 polls). */
+NS_API int ns_tma_wait_test(int device, long long spin_limit);
+
 /*
  * Batched sweeps: many independent Euler instances (inviscid = 1, nk = 4,
  * base flow uniform in x with v = 0 and uniform p; each with its own size,

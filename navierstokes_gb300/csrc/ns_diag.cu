@@ -4,11 +4,15 @@
 // host arrays, for testing them against the library functions.
 // ns_transport_eval: mu(T), k(T) as a context's k_first evaluates them.
 //
+// ns_tma_wait_test: the bounded mbarrier wait of the TMA tile loads, made to
+// run out (a barrier whose bytes never arrive), for testing the error path.
+//
 // ns_fp64_peak: the FP64 FMA throughput of a device, measured with a
 // register-only DFMA loop (8 independent chains per thread, 4 blocks of 256
 // threads per SM).  On GB300 the FP64 pipe, not HBM, bounds the FP64 stage
 // kernels, so this is the denominator of their FP64 roofline fraction.
 #include "ns_internal.cuh"
+#include "ns_tma.cuh"
 
 namespace {
 
@@ -102,4 +106,39 @@ extern "C" int ns_transport_eval(ns_ctx *c, const double *T, double *mu, double 
         rc = NS_ERR_CUDA;
     cudaFree(d);
     return rc;
+}
+
+namespace {
+
+// One block: the barrier expects 64 bytes that no copy delivers, so every
+// thread's bounded wait runs out and sets the error word.
+__global__ void k_tma_wait_test(int *err, long long limit)
+{
+    __shared__ alignas(8) unsigned long long bar;
+    if (threadIdx.x == 0) {
+        ns::mbar_init(&bar, 1);
+        ns::mbar_expect_tx(&bar, 64);
+    }
+    __syncthreads();
+    ns::mbar_wait_bounded(&bar, 0, err, limit);
+}
+
+}  // namespace
+
+extern "C" int ns_tma_wait_test(int device, long long spin_limit)
+{
+    if (spin_limit < 1 || spin_limit > (1LL << 16)) return NS_ERR_PARAM;
+    if (cudaSetDevice(device) != cudaSuccess) return NS_ERR_CUDA;
+    int *d = nullptr;
+    if (cudaMalloc(&d, sizeof(int)) != cudaSuccess) return NS_ERR_OOM;
+    int h = 0;
+    cudaError_t e = cudaMemset(d, 0, sizeof(int));
+    if (e == cudaSuccess) {
+        k_tma_wait_test<<<1, 64>>>(d, spin_limit);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(&h, d, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return NS_ERR_CUDA;
+    return h ? NS_ERR_TIMEOUT : NS_OK;
 }

@@ -44,14 +44,14 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned 
     return done != 0;
 }
 
-// Waits for phase `parity` of the barrier at most kTmaSpinLimit polls.
+// Waits for phase `parity` of the barrier at most `limit` polls.
 // False: the wait gave up and `err` is set.
 __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsigned parity,
-                                                  int *err)
+                                                  int *err, long long limit = kTmaSpinLimit)
 {
     long long spins = 0;
     while (!mbar_try_wait(bar, parity)) {
-        if (++spins > kTmaSpinLimit) {
+        if (++spins > limit) {
             atomicExch(err, 1);
             return false;
         }
