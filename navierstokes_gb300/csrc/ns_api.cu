@@ -367,7 +367,7 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
 }
 
 // TMA map of one perturbation buffer: planes of jmax rows of fpitch floats;
-// box 40 x 22 x planes (the stage kernel's halo tile)
+// box 40 x (kSplitTY + 6) x planes (the stage kernel's halo tile)
 int make_split_map(ns_ctx *c, CUtensorMap *map, float *base, int planes)
 {
     const auto encode = tensor_map_encoder();
@@ -376,7 +376,7 @@ int make_split_map(ns_ctx *c, CUtensorMap *map, float *base, int planes)
     const cuuint64_t dims[3] = {(cuuint64_t)d.imax, (cuuint64_t)d.jmax, (cuuint64_t)planes};
     const cuuint64_t strides[2] = {(cuuint64_t)c->sp.fpitch * sizeof(float),
                                    (cuuint64_t)c->sp.fpitch * d.jmax * sizeof(float)};
-    const cuuint32_t box[3] = {40u, 22u, (cuuint32_t)planes};
+    const cuuint32_t box[3] = {40u, (cuuint32_t)(ns::kSplitTY + 6), (cuuint32_t)planes};
     const cuuint32_t estr[3] = {1u, 1u, 1u};
     const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box,
                               estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,

@@ -87,6 +87,11 @@ __device__ __forceinline__ double dline(const double *__restrict__ f, long long 
 constexpr int kFirstBX = 32, kFirstBY = 8;
 constexpr int kFirstTileL = 4, kFirstTileW = 40, kFirstTileH = kFirstBY + 6;
 
+// Split-precision stage kernel: blocks of 32 x kSplitTY points (8 thread
+// rows, kSplitTY/8 points per thread), at least kSplitMinBlocks resident per
+// SM; its TMA box is 40 x (kSplitTY + 6) x planes.
+constexpr int kSplitTY = 16, kSplitMinBlocks = 4;
+
 // Transport law mu(T), k(T) (coefficients.f90:27-59) as piecewise
 // polynomials in T: T = 2^e (1 + (j + f)/256), e in [kTrEmin, kTrEmin +
 // kTrOctaves), j the top 8 fraction bits; piece (e, j) holds kTrDeg+1

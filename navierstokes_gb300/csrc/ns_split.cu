@@ -100,7 +100,8 @@ __device__ __forceinline__ void d2f_split(double x, float &hi, float &lo)
 // Fused stage kernel: FP32 derivatives from a shared-memory tile, Euler RHS,
 // FP64 LDDRK update, buffer damping.  Out of place (qin -> qout).
 // ---------------------------------------------------------------------------
-constexpr int kTX = 32, kTY = 16, kH = 3;
+constexpr int kTX = 32, kTY = kSplitTY, kH = 3;
+constexpr int kPT = kTY / 8;  // points per thread (8 thread rows)
 constexpr int kSH = kTY + 2 * kH;
 // Tile width in shared memory: the TMA box starts 4 columns left of the
 // block (its x coordinate times 4 bytes must be a multiple of 16) and spans
@@ -177,7 +178,7 @@ __device__ __forceinline__ void pair_scale(float &h, float &l, float s)
 }
 
 template <int NP, bool FIRST, bool SRC>
-__global__ void __launch_bounds__(256, 4)
+__global__ void __launch_bounds__(256, kSplitMinBlocks)
     k_split_stage(const __grid_constant__ CUtensorMap qmap, int *__restrict__ err, Dims d,
                   int fpitch, const float *__restrict__ qin, float *__restrict__ qout,
                   double *__restrict__ W, const float *__restrict__ xc,
@@ -197,17 +198,17 @@ __global__ void __launch_bounds__(256, 4)
     if (lead) mbar_init(&tbar, 1);
     __syncthreads();
     if (lead) {
-        // the box (40 x 22 x NPL floats) starts at (i0-4, j0-3, 0); points
+        // the box (40 x kSH x NPL floats) starts at (i0-4, j0-3, 0); points
         // outside the grid read as zero and are never used
         mbar_expect_tx(&tbar, (unsigned)sizeof(sq));
         tma_load_3d(&sq[0][0][0], &qmap, i0 - kTL, j0 - kH, 0, &tbar);
     }
     // the FP64 accumulators of this thread's two points, requested before
     // the tile so that their latency overlaps the tile load
-    double wold[2][4];
+    double wold[kPT][4];
     if (!FIRST) {
 #pragma unroll
-        for (int h = 0; h < 2; h++) {
+        for (int h = 0; h < kPT; h++) {
             const int j = j0 + ty + 8 * h, i = i0 + tx;
             const bool ok = i < d.imax && j < d.jmax;
             const long long didx = (long long)j * d.pitch + i;
@@ -226,7 +227,7 @@ __global__ void __launch_bounds__(256, 4)
     const float clx4 = cxlp[4], clx5 = cxlp[5], clx6 = cxlp[6];
     const bool xint = (i >= 3 && i < d.imax - 3);
 #pragma unroll
-    for (int h = 0; h < 2; h++) {
+    for (int h = 0; h < kPT; h++) {
         const int ly = ty + 8 * h;
         const int j = j0 + ly;
         if (j >= d.jmax) break;
