@@ -243,6 +243,15 @@ NS_API int ns_transport_eval(ns_ctx *ctx, const double *T, double *mu, double *k
  * kernels do (their limit is 2^24 polls). */
 NS_API int ns_tma_wait_test(int device, long long spin_limit);
 
+/* Library diagnostic, host only: the piecewise-polynomial table of mu(T),
+ * k(T) that ns_create builds for a viscous context (Tref, fits {A,B,C,D} of
+ * mu and k).  Writes NS_TRANSPORT_TABLE_DOUBLES doubles: piece (e, j) for
+ * T = 2^e (1 + (j + f)/256), e = -2 .. 2, at (e + 2)*256 + j, holding six
+ * coefficients of mu then six of k in powers of u = T - 2^e (1 + j/256). */
+#define NS_TRANSPORT_TABLE_DOUBLES (5 * 256 * 12)
+NS_API int ns_transport_table(double Tref, const double *fit_mu, const double *fit_k,
+                              double *out);
+
 /*
  * Batched sweeps: many independent Euler instances (inviscid = 1, nk = 4,
  * base flow uniform in x with v = 0 and uniform p; each with its own size,

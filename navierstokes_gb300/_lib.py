@@ -25,6 +25,7 @@ NS_LAYOUT_ROWS = 2
 NS_PREC_FP64 = 0
 NS_PREC_SPLIT = 1
 NS_PREC_SPLIT32 = 2
+NS_TRANSPORT_TABLE_DOUBLES = 5 * 256 * 12
 NS_SRC_NONE = 0
 NS_SRC_GAUSSIAN = 1
 NS_SRC_FIELD = 2
@@ -61,6 +62,7 @@ SIGNATURES = [
     ("ns_transport_eval", C.c_int, [_VP, _VP, _VP, _VP, C.c_int]),
     ("ns_adjoint_stored_bytes", C.c_int, [_VP, C.POINTER(C.c_int64)]),
     ("ns_tma_wait_test", C.c_int, [C.c_int, C.c_longlong]),
+    ("ns_transport_table", C.c_int, [C.c_double, _VP, _VP, _VP]),
     ("ns_step_noalloc", C.c_int, [_VP, _VP, C.c_int64, C.c_int, C.c_int, _VP]),
     ("ns_batch_create", C.c_int, [_VP, C.c_int, C.c_int, C.POINTER(_VP)]),
     ("ns_batch_destroy", None, [_VP]),

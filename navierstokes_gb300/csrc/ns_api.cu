@@ -610,6 +610,17 @@ namespace ns {
 void record_error(const char *msg) { g_last_error = msg; }
 }  // namespace ns
 
+int ns_transport_table(double Tref, const double *fit_mu, const double *fit_k, double *out)
+{
+    static_assert(NS_TRANSPORT_TABLE_DOUBLES == ns::kTrPieces * ns::kTrStride, "table size");
+    if (!fit_mu || !fit_k || !out || !(Tref > 0.0))
+        return set_err(nullptr, NS_ERR_PARAM, "ns_transport_table: bad argument");
+    std::vector<double> tab;
+    ns::build_transport_table(tab, Tref, fit_mu, fit_k);
+    std::memcpy(out, tab.data(), tab.size() * sizeof(double));
+    return NS_OK;
+}
+
 extern "C" {
 
 int ns_abi_version(void) { return NS_ABI_VERSION; }
