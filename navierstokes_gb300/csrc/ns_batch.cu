@@ -495,10 +495,13 @@ __device__ void fy_item(const Args &a, int4 item, const T *srcq, T *dstq)
 }
 
 // Phase B: x lines of 32 consecutive rows, staged through shared memory
-// PW positions at a time (coalesced row segments).
+// PW positions at a time (coalesced row segments).  The copies go by
+// cp.async into two tiles, the next block's in flight while the current
+// block is filtered; each step leaves its output in the tile column it read,
+// and the tile goes back with row writes.
 template <typename T, int PW>
-__device__ void fx_item(const Args &a, int4 item, const T *srcq, T *dstq, T (*ti)[PW + 1],
-                        T (*to)[PW + 1])
+__device__ void fx_item(const Args &a, int4 item, const T *srcq, T *dstq,
+                        T (*tbuf)[32][PW + 1])
 {
     const Inst in = a.inst[item.x];
     const int lane = threadIdx.x & 31;
@@ -516,6 +519,18 @@ __device__ void fx_item(const Args &a, int4 item, const T *srcq, T *dstq, T (*ti
     const bool exact = (c == 0 || warm < 0 || a0 - warm <= 6);
     const int q0 = exact ? 6 : a0 - warm;
     const FCoef<T> fc = fcoef<T>(a, 0);
+    // copies of the block starting at step qb (positions qb+7 ..) into tile buf
+    auto issue = [&](int buf, int qb) {
+        const int pin = qb + 7;
+        for (int r = 0; r < nrows; r++)
+            for (int x = lane; x < PW; x += 32) {
+                const int pos = pin + x;
+                const bool ok = pos < n;
+                cp_async_elem(&tbuf[buf][r][x], sb + (long long)r * in.pitch + (ok ? pos : 0), ok);
+            }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    if (q0 < b0) issue(0, q0);
     T w[13];
     if (exact) {
 #pragma unroll
@@ -528,32 +543,36 @@ __device__ void fx_item(const Args &a, int4 item, const T *srcq, T *dstq, T (*ti
 #pragma unroll
         for (int t = 0; t < 13; t++) w[t] = s[q0 - 6 + t];
     }
+    int buf = 0;
     for (int qb = q0; qb < b0; qb += PW) {
-        const int pin = qb + 7;
-        for (int r = 0; r < nrows; r++)
-            for (int x = lane; x < PW; x += 32) {
-                const int pos = pin + x;
-                ti[r][x] = (pos < n) ? sb[(long long)r * in.pitch + pos] : T(0);
-            }
+        if (qb + PW < b0) {
+            issue(buf ^ 1, qb + PW);
+            tile_wait<1>();  // this block's copies have landed
+        } else {
+            tile_wait<0>();
+        }
         __syncwarp();
+        T(*tb)[PW + 1] = tbuf[buf];
         const int nstep = min(PW, b0 - qb);
         for (int t = 0; t < nstep; t++) {
             const T v = pass2<T>(w, fc.m);
-            to[lane][t] = v;
+            const T nxt = tb[lane][t];
+            tb[lane][t] = v;
 #pragma unroll
             for (int u = 0; u < 5; u++) w[u] = w[u + 1];
             w[5] = v;
 #pragma unroll
             for (int u = 6; u < 12; u++) w[u] = w[u + 1];
-            w[12] = ti[lane][t];
+            w[12] = nxt;
         }
         __syncwarp();
         for (int r = 0; r < nrows; r++)
             for (int x = lane; x < PW; x += 32) {
                 const int qq = qb + x;
-                if (x < nstep && qq >= a0) ob[(long long)r * in.pitch + qq] = to[r][x];
+                if (x < nstep && qq >= a0) ob[(long long)r * in.pitch + qq] = tb[r][x];
             }
         __syncwarp();
+        buf ^= 1;
     }
     if (c == chunks - 1 && active) {
 #pragma unroll
@@ -643,8 +662,8 @@ __global__ void __launch_bounds__(256) k_batch_step(Args a)
     extern __shared__ __align__(16) unsigned char smem[];
     constexpr int PW = sizeof(T) == 4 ? 32 : 16;
     const int warp = threadIdx.x >> 5;
-    T(*ti)[PW + 1] = reinterpret_cast<T(*)[PW + 1]>(smem) + (size_t)warp * 2 * 32;
-    T(*to)[PW + 1] = ti + 32;
+    // this warp's two x-line tiles of 32 rows
+    T(*tx2)[32][PW + 1] = reinterpret_cast<T(*)[32][PW + 1]>(smem) + (size_t)warp * 2;
     const long long nwarps = (long long)gridDim.x * kWarps;
     const long long gw = (long long)blockIdx.x * kWarps + warp;
     for (int st = 0; st < 6; st++) {
@@ -673,7 +692,7 @@ __global__ void __launch_bounds__(256) k_batch_step(Args a)
         }
         if (!grid_barrier(a)) return;
         for_items(a.work + 2 * st, a.nfx,
-                  [&](int wi) { fx_item<T, PW>(a, a.fx[wi], qb, qa, ti, to); });
+                  [&](int wi) { fx_item<T, PW>(a, a.fx[wi], qb, qa, tx2); });
         if (!grid_barrier(a)) return;
         for_items(a.work + 2 * st + 1, a.nfy, [&](int wi) { fy_item<T>(a, a.fy[wi], qa, qb); });
         if (!grid_barrier(a)) return;
