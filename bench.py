@@ -329,6 +329,31 @@ def split_study(args, local, hbm_peak):
     return out
 
 
+def small_grid_study(local, steps=500):
+    """The 201x201 Euler acoustic pulse (nk = 5), 500 steps from rest: the
+    L2-resident, latency-bound case.  Device-resident FP64 steps through the
+    step graph, timed with CUDA events."""
+    import torch
+    from navierstokes_gb300 import Solver, cases
+    c = cases.acoustic_pulse_case()
+    with Solver(c, device=local) as s:
+        stream = torch.cuda.Stream()
+        s.set_stream(stream.cuda_stream)
+        s.set_state(c.U0)
+        s.step(0, 20)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        s.step(20, steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+    return {"workload": f"Euler {c.imax}x{c.jmax} acoustic pulse, nk = {c.nk}, FP64",
+            "value": c.points / (ms * 1e-3) / 1e6, "unit": UNIT, "ms_per_step": ms,
+            "steps": steps}
+
+
 def batch_study(args, local):
     """The parameter-sweep workload: 64 independent Euler instances, sizes log-uniform in
     [128, 1024] (multiples of 32), monopole sources, mean flow M ~ U[0, 0.6],
@@ -626,6 +651,13 @@ def run_ours(args, world, rank, local, pg):
         except Exception as e:
             split = {"failed": str(e)}
 
+    small = None
+    if rank == 0 and world == 1:
+        try:
+            small = small_grid_study(local)
+        except Exception as e:
+            small = {"failed": str(e)}
+
     batched = None
     if rank == 0 and world == 1 and not args.no_batch:
         try:
@@ -672,6 +704,8 @@ def run_ours(args, world, rank, local, pg):
             line["cpu_baseline"] = cpu
         if split is not None:
             line["split_precision"] = split
+        if small is not None:
+            line["small_grid"] = small
         if batched is not None:
             line["batched"] = batched
         if adjoint is not None:
