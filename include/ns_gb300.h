@@ -249,6 +249,14 @@ NS_API int ns_tma_wait_test(int device, long long spin_limit);
  * T = 2^e (1 + (j + f)/256), e = -2 .. 2, at (e + 2)*256 + j, holding six
  * coefficients of mu then six of k in powers of u = T - 2^e (1 + j/256). */
 #define NS_TRANSPORT_TABLE_DOUBLES (5 * 256 * 12)
+
+/* Library diagnostic, host only: the launch shape of an FP64 filter sweep
+ * over nlines lines (per variable, nk variables) of n points with a warm-up
+ * of `warm` points on a device of nsm multiprocessors: every warp takes
+ * *seg consecutive pass-2 positions of the warp-lines (32 lines of one
+ * variable) laid end to end; *blocks blocks of 128 threads. */
+NS_API int ns_filter_plan(int nlines, int n, int nk, int warm, int nsm, int64_t *seg,
+                          int *blocks);
 NS_API int ns_transport_table(double Tref, const double *fit_mu, const double *fit_k,
                               double *out);
 

@@ -610,6 +610,18 @@ namespace ns {
 void record_error(const char *msg) { g_last_error = msg; }
 }  // namespace ns
 
+int ns_filter_plan(int nlines, int n, int nk, int warm, int nsm, int64_t *seg, int *blocks)
+{
+    if (nlines < 1 || n < 13 || nk < 1 || nsm < 1 || !seg || !blocks)
+        return set_err(nullptr, NS_ERR_PARAM, "ns_filter_plan: bad argument");
+    long long s = 0;
+    unsigned b = 0;
+    ns::filter_shape(nlines, n, nk, warm, nsm, ns::kFilterWarpsPerSmsp, s, b);
+    *seg = s;
+    *blocks = (int)b;
+    return NS_OK;
+}
+
 int ns_transport_table(double Tref, const double *fit_mu, const double *fit_k, double *out)
 {
     static_assert(NS_TRANSPORT_TABLE_DOUBLES == ns::kTrPieces * ns::kTrStride, "table size");
