@@ -167,6 +167,12 @@ NS_API int ns_synchronize(ns_ctx *ctx);
  * it in place from the GPU.  Returns when U holds the new state. */
 NS_API int ns_rk_euler(ns_ctx *ctx, double *U, double t, int iter, int nk);
 
+/* Page-locks (and releases) an existing host array, e.g. the Fortran U, so
+ * that ns_rk_euler takes the page-locked path on it (cudaHostRegister on
+ * the current device's context; `bytes` from the start of the array). */
+NS_API int ns_pin_host(void *p, size_t bytes);
+NS_API int ns_unpin_host(void *p);
+
 /* Reads U(1..nk) at np points (1-based i, j) into out[np*nk] (point-major):
  * the probe writes of euler.f90:156-161 without a full download. */
 NS_API int ns_get_probes(ns_ctx *ctx, int np, const int32_t *pi, const int32_t *pj,

@@ -610,6 +610,30 @@ namespace ns {
 void record_error(const char *msg) { g_last_error = msg; }
 }  // namespace ns
 
+int ns_pin_host(void *p, size_t bytes)
+{
+    if (!p || bytes == 0) return set_err(nullptr, NS_ERR_PARAM, "ns_pin_host: bad argument");
+    const cudaError_t e = cudaHostRegister(p, bytes, cudaHostRegisterDefault);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(nullptr, NS_ERR_CUDA, "ns_pin_host: cudaHostRegister: %s",
+                       cudaGetErrorString(e));
+    }
+    return NS_OK;
+}
+
+int ns_unpin_host(void *p)
+{
+    if (!p) return set_err(nullptr, NS_ERR_PARAM, "ns_unpin_host: NULL");
+    const cudaError_t e = cudaHostUnregister(p);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(nullptr, NS_ERR_CUDA, "ns_unpin_host: cudaHostUnregister: %s",
+                       cudaGetErrorString(e));
+    }
+    return NS_OK;
+}
+
 int ns_filter_plan(int nlines, int n, int nk, int warm, int nsm, int64_t *seg, int *blocks)
 {
     if (nlines < 1 || n < 13 || nk < 1 || nsm < 1 || !seg || !blocks)

@@ -166,6 +166,27 @@ def test_rk_euler_pinned_host_reads_directly(nslib, precision):
     assert not np.array_equal(pinned, c.U0)
 
 
+def test_rk_euler_on_registered_host_array(nslib):
+    """An existing host array (as a Fortran U would be) page-locked with
+    ns_pin_host takes the banded path of ns_rk_euler; results equal the
+    pageable path's bit for bit, and ns_unpin_host releases it."""
+    from navierstokes_gb300 import Solver
+    c = cases.mixing_layer_case(imax=96, jmax=200, D=10)
+    U = np.ascontiguousarray(c.U0.copy())
+    paged = c.U0.copy()
+    assert nslib.ns_pin_host(U.ctypes.data, U.nbytes) == 0
+    try:
+        with Solver(c) as s:
+            for it in range(3):
+                s.rk_euler(U, (it + 1) * c.dt, it)
+    finally:
+        assert nslib.ns_unpin_host(U.ctypes.data) == 0
+    with Solver(c) as s:
+        for it in range(3):
+            s.rk_euler(paged, (it + 1) * c.dt, it)
+    assert np.array_equal(U, paged)
+
+
 def test_probes_and_layouts(nslib):
     from navierstokes_gb300 import Solver
     c = cases.acoustic_pulse_case(imax=50, jmax=40, D=8)
