@@ -652,7 +652,7 @@ def run_ours(args, world, rank, local, pg):
             split = {"failed": str(e)}
 
     small = None
-    if rank == 0 and world == 1:
+    if rank == 0 and world == 1 and not args.no_small_grid:
         try:
             small = small_grid_study(local)
         except Exception as e:
@@ -728,6 +728,8 @@ def main():
     ap.add_argument("--no-split", action="store_true",
                     help="skip the split-precision study (Euler 4096^2)")
     ap.add_argument("--split-n", type=int, default=4096)
+    ap.add_argument("--no-small-grid", action="store_true",
+                    help="skip the 201x201 Euler pulse timing")
     ap.add_argument("--no-batch", action="store_true",
                     help="skip the batched-sweep study (64 instances)")
     ap.add_argument("--batch-n", type=int, default=64)
