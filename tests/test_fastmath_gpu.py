@@ -61,8 +61,6 @@ def test_transport_table(nslib):
     """mu(T), k(T) as the first-derivative kernel evaluates them: the
     piecewise-polynomial table over T in [1/4, 8), exp and log outside it,
     against the law evaluated in extended precision."""
-    import ctypes as C
-
     from navierstokes_gb300.cases import N2_FIT, acoustic_pulse_case
     from navierstokes_gb300.solver import Solver
 

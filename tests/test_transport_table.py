@@ -2,8 +2,6 @@
 (coefficients.f90:27-59, divided by mu0 and k0) that viscous contexts use,
 built on the host (no GPU) and evaluated here in extended precision against
 the law itself."""
-import ctypes as C
-
 import numpy as np
 import pytest
 
