@@ -42,9 +42,10 @@ UNIT = "Mpt-steps/s"
 #   k_filter_*: U in, U out
 BYTES_PER_POINT = {"k_prim": 32, "k_first": 144, "k_update": 240, "k_filter_x": 64,
                    "k_filter_y": 64, "k_bc": 0, "k_stage_sin": 0}
-# FP64 work per grid point of one launch, from the ncu instruction counts of
-# profiles/fp64_counts_ns_2048x2048.md (nk = 4, Navier-Stokes): flops (2 per
-# DFMA, 1 per DADD/DMUL) and FP64-pipe thread instructions.
+# FP64 work per grid point of one launch, from ncu's executed-instruction
+# counts of each kernel on a 2048x2048 Navier-Stokes grid (nk = 4): flops (2
+# per DFMA, 1 per DADD/DMUL) and FP64-pipe thread instructions (DFMA, DADD,
+# DMUL and the FP32<->FP64 conversions, which share that pipe on GB300).
 FP64_FLOP_PER_POINT = {"k_prim": 12.0, "k_first": 113.15, "k_update": 111.43,
                        "k_filter_x": 90.15, "k_filter_y": 90.15}
 FP64_INST_PER_POINT = {"k_prim": 7.0, "k_first": 81.03, "k_update": 71.84,
@@ -53,7 +54,12 @@ FP64_INST_PER_POINT = {"k_prim": 7.0, "k_first": 81.03, "k_update": 71.84,
 # (2048x2048), scaled to a launch by the number of points.
 TRAFFIC_PER_POINT = {"k_prim": 21.3, "k_first": 129.9, "k_update": 230.5,
                      "k_filter_x": 61.7, "k_filter_y": 61.7}
-FP64_PEAK_FALLBACK_TFLOPS = 1.19  # DFMA throughput measured on GB300 (profiles/fp64_peak.md)
+# DFMA throughput of a register-only loop measured on a GB300 (1.68 DFMA per
+# clock per SM at 2.07 GHz), used when ns_fp64_peak() cannot run
+FP64_PEAK_FALLBACK_TFLOPS = 1.19
+# FP64-pipe thread instructions per point-step of the whole step (sum of the
+# per-launch counts above over the step's 36 launches, nk = 4)
+FP64_INST_PER_POINT_STEP = 1662
 STEP_BYTES_FUSED_MIN = 1536  # compulsory bytes per point-step of a fused FP64 design, nk = 4
 
 
@@ -178,6 +184,7 @@ def run_reference(args, world, rank):
     threads = os.cpu_count() or 1
     oracle.set_threads(threads)
     case = build_case(args)
+    config = workload_config(case)
     # one step of the full grid first, to size the sample
     o = oracle.Oracle(case)
     U = case.U0.copy()
@@ -203,14 +210,14 @@ def run_reference(args, world, rank):
     dt = time.perf_counter() - t0
     val = case.points * args.steps / dt / 1e6
     sample = (f"{args.steps} timed steps of a {case.imax}x{case.jmax} grid "
-              f"({'full grid' if jmax_s == args.jmax else 'rows cropped to bound the run'}), "
+              f"({'full grid' if jmax_s == args.jmax else f'rows cropped from {args.jmax} to bound the run; the rate is per point-step'}), "
               f"{threads} OpenMP threads")
     line = {"metric": METRIC, "value": val, "unit": UNIT, "impl": "reference",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic: analytic pulse + isentropic vortex on the stretched grid",
-            "config": workload_config(case, {"full_jmax": args.jmax}),
+            "config": config,
             "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0,
@@ -596,13 +603,14 @@ def run_ours(args, world, rank, local, pg):
     bytes_launch = BYTES_PER_POINT.get(dom, 0) * case.points
     achieved = bytes_launch / (dms * 1e-3) / 1e9
     trafficpp = TRAFFIC_PER_POINT.get(dom)
-    roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak,
-            "unit": "GB/s", "frac": achieved / hbm_peak,
-            "traffic": trafficpp * case.points if trafficpp else None,
-            "traffic_source": "ncu dram__bytes_read+write per point of a 2048x2048 capture, "
-                              "times the points of this launch",
-            "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})",
-            "bytes_per_launch": bytes_launch}
+    # The FP64 pipe binds every FP64 kernel (ncu: 83-89 % busy), so the
+    # headline roofline is that pipe: FP64-pipe thread instructions per second
+    # against the nominal 2 per clock per SM at the maximum SM clock.  The HBM
+    # figures of the same kernel stand beside it.
+    hbm = {"achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+           "bytes_per_launch": bytes_launch,
+           "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})"}
+    traffic = trafficpp * case.points if trafficpp else None
     fp64_peak = C.c_double(0.0)
     if solver.lib.ns_fp64_peak(local, C.byref(fp64_peak)) != 0 or fp64_peak.value <= 0:
         fp64_peak.value = FP64_PEAK_FALLBACK_TFLOPS
@@ -611,25 +619,30 @@ def run_ours(args, world, rank, local, pg):
         if fl:
             v["fp64_tflops"] = fl * case.points / (v["ms_per_launch"] * 1e-3) / 1e12
             v["fp64_frac"] = v["fp64_tflops"] / fp64_peak.value
-    fl = FP64_FLOP_PER_POINT.get(dom)
-    if fl:
-        tf = fl * case.points / (dms * 1e-3) / 1e12
-        ins = FP64_INST_PER_POINT[dom] * case.points / (dms * 1e-3) / 1e9
-        peak_ins = fp64_peak.value * 1e3 / 2.0
-        roof["fp64"] = {"achieved": tf, "peak": fp64_peak.value, "unit": "TFLOP/s",
-                        "frac": tf / fp64_peak.value, "flop_per_point": fl,
-                        "pipe_inst_per_s": ins * 1e9, "pipe_frac": ins / peak_ins,
-                        "peak_source": "ns_fp64_peak(): DFMA loop measured live on this GPU",
-                        "binding": "the FP64 pipe binds this kernel, not HBM"}
-        # nominal rate: 2 FP64 thread instructions per clock per SM at the
-        # maximum SM clock (the DFMA loop reaches about 1.7 on these parts)
-        nsm = torch.cuda.get_device_properties(local).multi_processor_count
-        if clocks.get("sm_max_mhz"):
-            nominal = 2.0 * nsm * clocks["sm_max_mhz"] * 1e6
-            roof["fp64"]["pipe_inst_per_s_nominal"] = nominal
-            roof["fp64"]["pipe_frac_nominal"] = ins * 1e9 / nominal
-    step_bytes = STEP_BYTES_FUSED_MIN * case.points
-    roof["step_hbm_frac_fused_min"] = step_bytes / (ms_step * 1e-3) / 1e9 / hbm_peak
+    nsm = torch.cuda.get_device_properties(local).multi_processor_count
+    sm_max_mhz = clocks.get("sm_max_mhz") or 2070.0
+    nominal_ins = 2.0 * nsm * sm_max_mhz * 1e6
+    ins = FP64_INST_PER_POINT[dom] * case.points / (dms * 1e-3)
+    tf = FP64_FLOP_PER_POINT[dom] * case.points / (dms * 1e-3) / 1e12
+    roof = {"bound": "fp64", "kernel": dom,
+            "achieved": ins / 1e9, "peak": nominal_ins / 1e9, "unit": "FP64-pipe Ginst/s",
+            "frac": ins / nominal_ins,
+            "peak_source": f"nominal: 2 FP64 thread instructions per clock per SM, {nsm} SMs "
+                           f"at {sm_max_mhz:.0f} MHz",
+            "inst_per_point": FP64_INST_PER_POINT[dom],
+            "traffic": traffic,
+            "traffic_source": "ncu dram__bytes_read+write per point of a 2048x2048 capture, "
+                              "times the points of this launch",
+            "hbm": hbm,
+            "fp64_flops": {"achieved": tf, "unit": "TFLOP/s",
+                           "flop_per_point": FP64_FLOP_PER_POINT[dom],
+                           "dfma_loop_peak": fp64_peak.value,
+                           "frac_of_dfma_loop": tf / fp64_peak.value,
+                           "peak_source": "ns_fp64_peak(): DFMA loop measured live on this GPU"},
+            "step": {"fp64_pipe_frac": FP64_INST_PER_POINT_STEP * case.points
+                     / (ms_step * 1e-3) / nominal_ins,
+                     "hbm_frac_fused_min": STEP_BYTES_FUSED_MIN * case.points
+                     / (ms_step * 1e-3) / 1e9 / hbm_peak}}
 
     # ---- end to end through the C ABI with host buffers -----------------
     Uh = torch.empty(case.U0.shape, dtype=torch.float64, pin_memory=True).numpy()

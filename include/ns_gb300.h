@@ -266,6 +266,17 @@ NS_API int ns_filter_plan(int nlines, int n, int nk, int warm, int nsm, int64_t 
 NS_API int ns_transport_table(double Tref, const double *fit_mu, const double *fit_k,
                               double *out);
 
+/* Library diagnostic, host only: the coefficient tables every setup path of
+ * the library uses, numbered as the oracle numbers them: 0 the interior DRP
+ * weights a(1..3), 1..3 the left closures at points 3, 2, 1 (a_dudx4, 5, 6),
+ * 4..6 the right closures (a_dudx4b, 5b, 6b) (init.f90:288-338); 7 the
+ * 13-point filter df(-6..6) (filtering.f90:54-66); 8 and 9 the boundary
+ * filter dfb(-1..5) in x (REAL(8), filtering.f90:25-31) and y (REAL(4),
+ * filtering.f90:114-120); 10..12 LDDRK alpha, beta and c_k (rk.f90:27-46).
+ * Writes the table to out (room for 16 doubles) and returns its length,
+ * or 0 for an unknown number. */
+NS_API int ns_coef_table(int which, double *out);
+
 /*
  * Batched sweeps: many independent Euler instances (inviscid = 1, nk = 4,
  * base flow uniform in x with v = 0 and uniform p; each with its own size,
@@ -433,28 +444,33 @@ NS_API int ns_run_euler(const char *dados_path, const char *outdir, int nk, int 
  * cudaMalloc failure in the middle of a run is not acceptable, a caller that
  * must not let an allocation synchronise the device between its own kernels).
  *
- * Advances the state U by nsteps calls of rk_euler (same kernels and results
- * as ns_step) without calling cudaMalloc, cudaFree or any allocating
- * library routine: every work array lives in one file-scope __device__
- * array of NS_NOALLOC_MAX_BYTES, which every GPU that loads the library keeps
- * until the process exits.  The caller passes the inputs and the output:
- * p as for ns_create (host arrays, read on every call), and U, the device
- * state: nk planes of jmax rows of `pitch` doubles (pitch >= imax, a
- * multiple of 32), updated in place.  stream: a cudaStream_t, NULL for the
- * default stream; the call returns once the work is enqueued.
+ * Advances the state U by nsteps calls of rk_euler without calling
+ * cudaMalloc, cudaFree or any allocating library routine: every work array,
+ * the transport-law table of a viscous case included, lives in one
+ * file-scope __device__ array of NS_NOALLOC_MAX_BYTES, which every GPU that
+ * loads the library keeps until the process exits.  The kernels are those of
+ * ns_step, with the halo tiles read from global memory instead of by TMA
+ * (the same arithmetic in the same order).  The caller passes the inputs and
+ * the output: p as for ns_create (host arrays, read on every call), and U,
+ * the device state: nk planes of jmax rows of `pitch` doubles (pitch >= imax,
+ * a multiple of 32), updated in place.  stream: a cudaStream_t, NULL for the
+ * default stream; the call returns once the work is enqueued.  The calling
+ * thread's current device is the same after the call as before it.
  *
- * Limits: imax, jmax <= NS_NOALLOC_MAX_LINE and about (5*nk+9)*pitch*jmax
- * doubles of work area (a 96x72 nk = 5 case uses 1.9 MB; 512x480 with
- * nk = 4 fits); larger cases are rejected with NS_ERR_PARAM and a message
- * giving the bytes needed.
+ * Limits: imax, jmax <= NS_NOALLOC_MAX_LINE, pitch <= NS_NOALLOC_MAX_BYTES/8,
+ * and about (5*nk+9)*pitch*jmax doubles of work area (a 96x72 nk = 5 case
+ * uses 1.9 MB; 512x480 with nk = 4 fits); larger cases are rejected with
+ * NS_ERR_PARAM and a message giving the bytes needed.
  *
  * The first call on a device finds the work area's device address
  * (cudaGetSymbolAddress, with that device current, which may also load the
- * module): make that first call before any stream capture.  Every call
- * shares the one work area and leaves its contents behind; each call writes
- * every part it reads, so results never depend on an earlier call, but calls
- * that overlap on the GPU (other streams, other host threads) race and must
- * be serialised by the caller.
+ * module).  Each call copies its setup tables from host memory that the next
+ * call reuses; a call made on a stream that is capturing returns
+ * NS_ERR_UNSUPPORTED without enqueueing anything.  Every call shares the
+ * one work area and leaves its contents behind; each call writes every part
+ * it reads, so results never depend on an earlier call, but calls that
+ * overlap on the GPU (other streams, other host threads) race and must be
+ * serialised by the caller.
  */
 #define NS_NOALLOC_MAX_BYTES (64u << 20)
 #define NS_NOALLOC_MAX_LINE 8192

@@ -63,6 +63,7 @@ SIGNATURES = [
     ("ns_adjoint_stored_bytes", C.c_int, [_VP, C.POINTER(C.c_int64)]),
     ("ns_tma_wait_test", C.c_int, [C.c_int, C.c_longlong]),
     ("ns_transport_table", C.c_int, [C.c_double, _VP, _VP, _VP]),
+    ("ns_coef_table", C.c_int, [C.c_int, _VP]),
     ("ns_pin_host", C.c_int, [_VP, C.c_size_t]),
     ("ns_unpin_host", C.c_int, [_VP]),
     ("ns_filter_plan", C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,

@@ -17,6 +17,7 @@
 #include <cudaTypedefs.h>
 #include <mutex>
 
+#include "ns_coef.h"
 #include "ns_internal.cuh"
 
 #define NS_STR2(x) #x
@@ -25,42 +26,17 @@
 
 namespace {
 
+using namespace ns::coef;
+
 thread_local std::string g_last_error;
 
-// DRP coefficients, init.f90:288-338.
-const double kA[3] = {0.770882380518, -0.166705904415, 0.0208431427703};
-const double kA4[7] = {0.049041958000, -0.46884035700, -0.47476091400, 1.27327473700,
-                       -0.51848452600, 0.16613853300,  -0.026369431000};
-const double kA4b[7] = {0.026369431000, -0.16613853300, 0.51848452600, -1.27327473700,
-                        0.47476091400,  0.46884035700,  -0.049041958000};
-const double kA5[7] = {-0.20933762200, -1.08487567600, 2.14777605000, -1.38892832200,
-                       0.76894976600,  -0.28181465000, 0.048230454000};
-const double kA5b[7] = {-0.048230454000, 0.28181465000,  -0.76894976600, 1.38892832200,
-                        -2.14777605000,  1.08487567600, 0.20933762200};
-const double kA6[7] = {-2.19228033900, 4.74861140100, -5.10885191500, 4.46156710400,
-                       -2.83349874100, 1.12832886100, -0.20387637100};
-const double kA6b[7] = {0.20387637100, -1.12832886100, 2.83349874100, -4.46156710400,
-                        5.10885191500, -4.74861140100, 2.19228033900};
-// Selective filter, filtering.f90:54-66 (df(0..6); symmetric).
-const double kDf[7] = {0.190899511506,  -0.171503832236, 0.123632891797, -0.069975429105,
-                       0.029662754736, -0.008520738659, 0.001254597714};
-// Boundary filter dfb(-1..5): REAL(8) literals in x (filtering.f90:25-31),
-// default-REAL (single precision) literals in y (filtering.f90:114-120).
-const double kDfbX[7] = {-0.057717512738, 0.199278374994,  -0.292668277650, 0.244537361546,
-                         -0.134605018019, 0.056184263460, -0.015009191593};
-const double kDfbY[7] = {(double)-0.057717512738f, (double)0.199278374994f,
-                         (double)-0.292668277650f, (double)0.244537361546f,
-                         (double)-0.134605018019f, (double)0.056184263460f,
-                         (double)-0.015009191593f};
-// LDDRK, rk.f90:27-46.
-const double kAlpha[6] = {0.0, -0.737101392796, -1.634740794341,
-                          -0.744739003780, -1.469897351522, -2.813971388035};
-const double kBeta[6] = {0.032918605146, 0.823256998200, 0.381530948900,
-                         0.200092213184, 1.718581042715, 0.27};
-const double kCt[6] = {0.0, 0.032918605146, 0.249351723343,
-                       0.466911705055, 0.582030414044, 0.847252983783};
-// global.f90:38-39
-const double kPe = 1000.0, kAlphaCond = 0.5;
+// Per-line derivative table as a vector (ns::coef::line_table).
+void build_coef(std::vector<double> &tab, int n, double h, const double *mesh, int D,
+                int metric_mode)
+{
+    tab.resize((size_t)n * ns::kCoefStride);
+    line_table(tab.data(), n, h, mesh, D, metric_mode);
+}
 
 int set_err(ns_ctx *c, int code, const char *fmt, ...)
 {
@@ -85,119 +61,6 @@ int cuda_err(ns_ctx *c, cudaError_t e, const char *what)
         if (e_ != cudaSuccess) return cuda_err((c), e_, #call);   \
     } while (0)
 
-// Per-line coefficient table (see ns::kCoefStride); mesh == NULL: no metric.
-void build_coef(std::vector<double> &tab, int n, double h, const double *mesh, int D,
-                int metric_mode)
-{
-    tab.assign((size_t)n * ns::kCoefStride, 0.0);
-    for (int q = 0; q < n; q++) {
-        double mt = 1.0;
-        if (!mesh)
-            mt = 1.0;
-        else if (metric_mode == NS_METRIC_EVERYWHERE)
-            mt = mesh[q];
-        else if (q < D || q >= n - D)
-            mt = mesh[q];
-        double *c = &tab[(size_t)q * ns::kCoefStride];
-        const double *src = nullptr;
-        if (q == 0) src = kA6;
-        else if (q == 1) src = kA5;
-        else if (q == 2) src = kA4;
-        else if (q == n - 3) src = kA4b;
-        else if (q == n - 2) src = kA5b;
-        else if (q == n - 1) src = kA6b;
-        if (src) {
-            for (int z = 0; z < 7; z++) c[z] = src[z] * mt / h;
-        } else {
-            for (int s = 0; s < 3; s++) c[4 + s] = kA[s] * mt / h;
-        }
-    }
-}
-
-ns::FilterCoef make_filter(double sigmaf, const double *dfb)
-{
-    ns::FilterCoef f;
-    std::memset(&f, 0, sizeof f);
-    f.c0 = 1.0 - sigmaf * kDf[0];
-    for (int s = 1; s <= 6; s++) f.m[s] = -sigmaf * kDf[s];
-    f.bm1 = -sigmaf * dfb[0];
-    f.b0 = 1.0 - sigmaf * dfb[1];
-    for (int s = 1; s <= 5; s++) f.b[s] = -sigmaf * dfb[s + 1];
-    return f;
-}
-
-// Warm-up length of the chunked filter recurrence: the number of points
-// after which the response of the homogeneous recurrence
-// e(q) = -sigmaf*sum_{s=1..6} df(s)*e(q-s) to any unit history has fallen
-// below 2^-60 for good, plus a margin.  -1 when it never does (the sweeps
-// then run serially, one chunk per line).
-int filter_warmup(double sigmaf)
-{
-    const int kMax = 4096;
-    const double thresh = std::ldexp(1.0, -60);
-    int worst = 0;
-    for (int u = 0; u < 6; u++) {
-        std::vector<double> e(kMax + 6, 0.0);
-        e[u] = 1.0;
-        int last_big = 0;
-        for (int q = 6; q < kMax + 6; q++) {
-            double v = 0.0;
-            for (int s = 1; s <= 6; s++) v += -sigmaf * kDf[s] * e[q - s];
-            e[q] = v;
-            if (std::fabs(v) >= thresh) last_big = q - 5;
-        }
-        if (last_big >= kMax - 64) return -1;
-        if (last_big > worst) worst = last_big;
-    }
-    int w = worst + 8;
-    if (w < 36) w = 36;
-    return w;
-}
-
-// Warm-up for a given decay threshold (2^-60 for FP64 results, 2^-32 for
-// the FP32 perturbation filters).
-int filter_warmup_thresh(double sigmaf, double thresh)
-{
-    const int kMax = 4096;
-    int worst = 0;
-    std::vector<double> e(kMax + 6);
-    for (int u = 0; u < 6; u++) {
-        std::fill(e.begin(), e.end(), 0.0);
-        e[u] = 1.0;
-        int last_big = 0;
-        for (int q = 6; q < kMax + 6; q++) {
-            double v = 0.0;
-            for (int s = 1; s <= 6; s++) v += -sigmaf * kDf[s] * e[q - s];
-            e[q] = v;
-            if (std::fabs(v) >= thresh) last_big = q - 5;
-        }
-        if (last_big >= kMax - 64) return -1;
-        if (last_big > worst) worst = last_big;
-    }
-    const int w = worst + 8;
-    return w < 16 ? 16 : w;
-}
-
-// The three in-place sweeps of lddfilterx/lddfiltery (filtering.f90:39-94)
-// on one line, serially, in FP64.
-void serial_filter_line(double *u, int n, double sigmaf, const double *dfb)
-{
-    for (int q = 1; q <= 6; q++) {
-        double Du = 0.0;
-        for (int s = -1; s <= 5; s++) Du += dfb[s + 1] * u[q + s];
-        u[q] -= sigmaf * Du;
-    }
-    for (int q = 6; q <= n - 7; q++) {
-        double Du = 0.0;
-        for (int s = -6; s <= 6; s++) Du += kDf[s < 0 ? -s : s] * u[q + s];
-        u[q] -= sigmaf * Du;
-    }
-    for (int q = n - 2; q >= n - 7; q--) {
-        double Du = 0.0;
-        for (int s = -1; s <= 5; s++) Du += dfb[s + 1] * u[q - s];
-        u[q] -= sigmaf * Du;
-    }
-}
 
 // DRP first derivative of a line with the per-position table (FP64).
 double line_derivative(const double *f, int q, int n, const double *c)
@@ -877,14 +740,14 @@ constants:
             ph.D_mi_s = p->D_mi - ami0;
             ph.D_k_s = p->D_k - ak0;
         }
-        c->fx = make_filter(p->sigmaf, kDfbX);
-        c->fy = make_filter(p->sigmaf, kDfbY);
+        c->fx = filter(p->sigmaf, kDfbX);
+        c->fy = filter(p->sigmaf, kDfbY);
         for (int k = 0; k < 6; k++) {
             c->ct[k] = kCt[k];
             c->alpha[k] = kAlpha[k];
             c->beta[k] = kBeta[k];
         }
-        c->warm = filter_warmup(p->sigmaf);
+        c->warm = warmup(p->sigmaf, std::ldexp(1.0, -60), 36);
         int nsm = 152;
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->dev);
         c->nsm = nsm;
@@ -892,7 +755,7 @@ constants:
             // FP32 filters are bound by memory: aim at 32 resident warps per SM
             ns::SplitState &sp = c->sp;
             // pairs carry ~48 bits: warm-up to 2^-50; single FP32 to 2^-32
-            sp.warm = filter_warmup_thresh(p->sigmaf, std::ldexp(1.0, sp.np ? -50 : -32));
+            sp.warm = warmup(p->sigmaf, std::ldexp(1.0, sp.np ? -50 : -32), 16);
             const int twarps = nsm * 32;
             const int xgroups = 4 * ((d.jmax + 31) / 32);
             sp.fx_chunks = choose_chunks(xgroups, d.imax, sp.warm, twarps);
@@ -1190,6 +1053,21 @@ int ns_step_launches(ns_ctx *c, int *launches)
     if (!c || !launches) return set_err(c, NS_ERR_PARAM, "ns_step_launches: NULL argument");
     *launches = c->launches_per_step;
     return NS_OK;
+}
+
+int ns_coef_table(int which, double *out)
+{
+    if (!out) return 0;
+    const double *const tabs[13] = {kA, kA4, kA5, kA6, kA4b, kA5b, kA6b, nullptr,
+                                    kDfbX, kDfbY, kAlpha, kBeta, kCt};
+    const int lens[13] = {3, 7, 7, 7, 7, 7, 7, 13, 7, 7, 6, 6, 6};
+    if (which < 0 || which > 12) return 0;
+    if (which == 7) {
+        for (int s = -6; s <= 6; s++) out[s + 6] = kDf[s < 0 ? -s : s];
+    } else {
+        for (int z = 0; z < lens[which]; z++) out[z] = tabs[which][z];
+    }
+    return lens[which];
 }
 
 int ns_filter_warmup(ns_ctx *c, int *warmup)

@@ -24,6 +24,7 @@
 #include <cstring>
 #include <vector>
 
+#include "ns_coef.h"
 #include "ns_internal.cuh"
 
 namespace ns {
@@ -787,31 +788,7 @@ struct ns_batch {
 
 namespace {
 
-const double kA[3] = {0.770882380518, -0.166705904415, 0.0208431427703};
-const double kA4[7] = {0.049041958000, -0.46884035700, -0.47476091400, 1.27327473700,
-                       -0.51848452600, 0.16613853300,  -0.026369431000};
-const double kA4b[7] = {0.026369431000, -0.16613853300, 0.51848452600, -1.27327473700,
-                        0.47476091400,  0.46884035700,  -0.049041958000};
-const double kA5[7] = {-0.20933762200, -1.08487567600, 2.14777605000, -1.38892832200,
-                       0.76894976600,  -0.28181465000, 0.048230454000};
-const double kA5b[7] = {-0.048230454000, 0.28181465000,  -0.76894976600, 1.38892832200,
-                        -2.14777605000,  1.08487567600, 0.20933762200};
-const double kA6[7] = {-2.19228033900, 4.74861140100, -5.10885191500, 4.46156710400,
-                       -2.83349874100, 1.12832886100, -0.20387637100};
-const double kA6b[7] = {0.20387637100, -1.12832886100, 2.83349874100, -4.46156710400,
-                        5.10885191500, -4.74861140100, 2.19228033900};
-const double kDf[7] = {0.190899511506,  -0.171503832236, 0.123632891797, -0.069975429105,
-                       0.029662754736, -0.008520738659, 0.001254597714};
-const double kDfbX[7] = {-0.057717512738, 0.199278374994,  -0.292668277650, 0.244537361546,
-                         -0.134605018019, 0.056184263460, -0.015009191593};
-const double kDfbY[7] = {(double)-0.057717512738f, (double)0.199278374994f,
-                         (double)-0.292668277650f, (double)0.244537361546f,
-                         (double)-0.134605018019f, (double)0.056184263460f,
-                         (double)-0.015009191593f};
-const double kAlpha[6] = {0.0, -0.737101392796, -1.634740794341,
-                          -0.744739003780, -1.469897351522, -2.813971388035};
-const double kBeta[6] = {0.032918605146, 0.823256998200, 0.381530948900,
-                         0.200092213184, 1.718581042715, 0.27};
+using namespace ns::coef;
 
 int berr(ns_batch *b, int code, const std::string &msg)
 {
@@ -822,58 +799,8 @@ int berr(ns_batch *b, int code, const std::string &msg)
 
 void coef_table(std::vector<double> &tab, int n, double h, const double *mesh, int D, int mode)
 {
-    tab.assign((size_t)n * ns::kCoefStride, 0.0);
-    for (int q = 0; q < n; q++) {
-        double mt = 1.0;
-        if (mode == NS_METRIC_EVERYWHERE || q < D || q >= n - D) mt = mesh[q];
-        double *c = &tab[(size_t)q * ns::kCoefStride];
-        const double *src = q == 0 ? kA6 : q == 1 ? kA5 : q == 2 ? kA4 : q == n - 3 ? kA4b
-                            : q == n - 2 ? kA5b : q == n - 1 ? kA6b : nullptr;
-        if (src)
-            for (int z = 0; z < 7; z++) c[z] = src[z] * mt / h;
-        else
-            for (int s = 0; s < 3; s++) c[4 + s] = kA[s] * mt / h;
-    }
-}
-
-void serial_filter(double *u, int n, double sigmaf, const double *dfb)
-{
-    for (int q = 1; q <= 6; q++) {
-        double Du = 0.0;
-        for (int s = -1; s <= 5; s++) Du += dfb[s + 1] * u[q + s];
-        u[q] -= sigmaf * Du;
-    }
-    for (int q = 6; q <= n - 7; q++) {
-        double Du = 0.0;
-        for (int s = -6; s <= 6; s++) Du += kDf[s < 0 ? -s : s] * u[q + s];
-        u[q] -= sigmaf * Du;
-    }
-    for (int q = n - 2; q >= n - 7; q--) {
-        double Du = 0.0;
-        for (int s = -1; s <= 5; s++) Du += dfb[s + 1] * u[q - s];
-        u[q] -= sigmaf * Du;
-    }
-}
-
-int warmup_len(double sigmaf, double thresh)
-{
-    const int kMax = 4096;
-    std::vector<double> e(kMax + 6);
-    int worst = 0;
-    for (int u = 0; u < 6; u++) {
-        std::fill(e.begin(), e.end(), 0.0);
-        e[u] = 1.0;
-        int last = 0;
-        for (int q = 6; q < kMax + 6; q++) {
-            double v = 0.0;
-            for (int s = 1; s <= 6; s++) v += -sigmaf * kDf[s] * e[q - s];
-            e[q] = v;
-            if (std::fabs(v) >= thresh) last = q - 5;
-        }
-        if (last >= kMax - 64) return -1;
-        worst = std::max(worst, last);
-    }
-    return std::max(worst + 8, 16);
+    tab.resize((size_t)n * ns::kCoefStride);
+    line_table(tab.data(), n, h, mesh, D, mode);
 }
 
 double line_deriv(const double *f, int q, int n, const double *c)
@@ -1094,8 +1021,8 @@ int ns_batch_create(const ns_params *const *params, int n, int precision, ns_bat
     long long qoff = 0, woff = 0, soff = 0;
     int xoff = 0, yoff = 0;
     double sigmaf = params[0]->sigmaf;
-    const int warm = warmup_len(sigmaf, precision == NS_PREC_SPLIT32 ? std::ldexp(1.0, -32)
-                                                                   : std::ldexp(1.0, -60));
+    const int warm = warmup(sigmaf, precision == NS_PREC_SPLIT32 ? std::ldexp(1.0, -32)
+                                                               : std::ldexp(1.0, -60), 16);
     for (int q = 0; q < n && rc == NS_OK; q++) {
         const ns_params *p = params[q];
         const int imax = p->imax, jmax = p->jmax;
@@ -1178,7 +1105,7 @@ int ns_batch_create(const ns_params *const *params, int n, int precision, ns_bat
         for (int k = 0; k < 4; k++) {
             for (int j = 0; j < jmax; j++) col[j] = k == 0 ? rj[j] : k == 1 ? uj2[j] : k == 2 ? 0.0 : pb;
             f = col;
-            serial_filter(f.data(), jmax, sigmaf, kDfbY);
+            serial_filter_line(f.data(), jmax, sigmaf, kDfbY);
             for (int j = 0; j < jmax; j++) corr.push_back(f[j] - col[j]);
         }
         b->hpmean.push_back(pb);

@@ -22,10 +22,14 @@
 #include <cstdio>
 #include <cstring>
 #include <mutex>
+#include <vector>
 
+#include "ns_coef.h"
 #include "ns_internal.cuh"
 
 namespace {
+
+using namespace ns::coef;
 
 constexpr size_t kScratchDoubles = NS_NOALLOC_MAX_BYTES / sizeof(double);
 constexpr int kMaxDevices = 64;
@@ -36,42 +40,13 @@ static __device__ __align__(256) double g_noalloc_work[kScratchDoubles];
 
 std::mutex g_mu;
 double *g_work_ptr[kMaxDevices];       // device address of g_noalloc_work, per device
-// host staging for the per-line tables (serialised by g_mu)
+// host staging for the per-line tables and the transport-law table
+// (serialised by g_mu)
 double g_hx[ns::kCoefStride * NS_NOALLOC_MAX_LINE];
 double g_hy[ns::kCoefStride * NS_NOALLOC_MAX_LINE];
-double g_warm_e[4096 + 6];
-
-// Same tables as the context path (ns_api.cu): DRP coefficients
-// init.f90:288-338, filters filtering.f90:25-31, :54-66, :114-120,
-// LDDRK rk.f90:27-46, constants global.f90:38-39.
-const double kA[3] = {0.770882380518, -0.166705904415, 0.0208431427703};
-const double kA4[7] = {0.049041958000, -0.46884035700, -0.47476091400, 1.27327473700,
-                       -0.51848452600, 0.16613853300,  -0.026369431000};
-const double kA4b[7] = {0.026369431000, -0.16613853300, 0.51848452600, -1.27327473700,
-                        0.47476091400,  0.46884035700,  -0.049041958000};
-const double kA5[7] = {-0.20933762200, -1.08487567600, 2.14777605000, -1.38892832200,
-                       0.76894976600,  -0.28181465000, 0.048230454000};
-const double kA5b[7] = {-0.048230454000, 0.28181465000,  -0.76894976600, 1.38892832200,
-                        -2.14777605000,  1.08487567600, 0.20933762200};
-const double kA6[7] = {-2.19228033900, 4.74861140100, -5.10885191500, 4.46156710400,
-                       -2.83349874100, 1.12832886100, -0.20387637100};
-const double kA6b[7] = {0.20387637100, -1.12832886100, 2.83349874100, -4.46156710400,
-                        5.10885191500, -4.74861140100, 2.19228033900};
-const double kDf[7] = {0.190899511506,  -0.171503832236, 0.123632891797, -0.069975429105,
-                       0.029662754736, -0.008520738659, 0.001254597714};
-const double kDfbX[7] = {-0.057717512738, 0.199278374994,  -0.292668277650, 0.244537361546,
-                         -0.134605018019, 0.056184263460, -0.015009191593};
-const double kDfbY[7] = {(double)-0.057717512738f, (double)0.199278374994f,
-                         (double)-0.292668277650f, (double)0.244537361546f,
-                         (double)-0.134605018019f, (double)0.056184263460f,
-                         (double)-0.015009191593f};
-const double kAlpha[6] = {0.0, -0.737101392796, -1.634740794341,
-                          -0.744739003780, -1.469897351522, -2.813971388035};
-const double kBeta[6] = {0.032918605146, 0.823256998200, 0.381530948900,
-                         0.200092213184, 1.718581042715, 0.27};
-const double kCt[6] = {0.0, 0.032918605146, 0.249351723343,
-                       0.466911705055, 0.582030414044, 0.847252983783};
-const double kPe = 1000.0, kAlphaCond = 0.5;
+double g_tr[ns::kTrPieces * ns::kTrStride];
+double g_tr_key[9];                    // Tref and the two fits g_tr was built for
+bool g_tr_valid = false;
 
 int fail(int code, const char *fmt, ...) __attribute__((format(printf, 2, 3)));
 int fail(int code, const char *fmt, ...)
@@ -85,60 +60,25 @@ int fail(int code, const char *fmt, ...)
     return code;
 }
 
-void fill_coef(double *tab, int n, double h, const double *mesh, int D, int metric_mode)
-{
-    std::memset(tab, 0, sizeof(double) * ns::kCoefStride * (size_t)n);
-    for (int q = 0; q < n; q++) {
-        double mt = 1.0;
-        if (metric_mode == NS_METRIC_EVERYWHERE || q < D || q >= n - D) mt = mesh[q];
-        double *c = tab + (size_t)q * ns::kCoefStride;
-        const double *src = nullptr;
-        if (q == 0) src = kA6;
-        else if (q == 1) src = kA5;
-        else if (q == 2) src = kA4;
-        else if (q == n - 3) src = kA4b;
-        else if (q == n - 2) src = kA5b;
-        else if (q == n - 1) src = kA6b;
-        if (src)
-            for (int z = 0; z < 7; z++) c[z] = src[z] * mt / h;
-        else
-            for (int s = 0; s < 3; s++) c[4 + s] = kA[s] * mt / h;
-    }
-}
+// Puts the calling thread's current device back on every return path.
+struct DeviceGuard {
+    int prev = -1;
+    DeviceGuard() { if (cudaGetDevice(&prev) != cudaSuccess) prev = -1; }
+    ~DeviceGuard() { if (prev >= 0) cudaSetDevice(prev); }
+};
 
-ns::FilterCoef filter_coef(double sigmaf, const double *dfb)
+// The transport-law table of ns_create for these constants, rebuilt only
+// when they change (building it takes a few milliseconds).
+void transport_table(const ns_params *p)
 {
-    ns::FilterCoef f;
-    std::memset(&f, 0, sizeof f);
-    f.c0 = 1.0 - sigmaf * kDf[0];
-    for (int s = 1; s <= 6; s++) f.m[s] = -sigmaf * kDf[s];
-    f.bm1 = -sigmaf * dfb[0];
-    f.b0 = 1.0 - sigmaf * dfb[1];
-    for (int s = 1; s <= 5; s++) f.b[s] = -sigmaf * dfb[s + 1];
-    return f;
-}
-
-// Warm-up of the chunked filter recurrence (same rule as the context path).
-int warmup(double sigmaf)
-{
-    const int kMax = 4096;
-    const double thresh = std::ldexp(1.0, -60);
-    int worst = 0;
-    for (int u = 0; u < 6; u++) {
-        std::memset(g_warm_e, 0, sizeof g_warm_e);
-        g_warm_e[u] = 1.0;
-        int last_big = 0;
-        for (int q = 6; q < kMax + 6; q++) {
-            double v = 0.0;
-            for (int s = 1; s <= 6; s++) v += -sigmaf * kDf[s] * g_warm_e[q - s];
-            g_warm_e[q] = v;
-            if (std::fabs(v) >= thresh) last_big = q - 5;
-        }
-        if (last_big >= kMax - 64) return -1;
-        if (last_big > worst) worst = last_big;
-    }
-    const int w = worst + 8;
-    return w < 36 ? 36 : w;
+    const double key[9] = {p->Tref, p->A_mi, p->B_mi, p->C_mi, p->D_mi,
+                           p->A_k,  p->B_k,  p->C_k,  p->D_k};
+    if (g_tr_valid && std::memcmp(key, g_tr_key, sizeof key) == 0) return;
+    std::vector<double> tab;
+    ns::build_transport_table(tab, p->Tref, key + 1, key + 5);
+    std::memcpy(g_tr, tab.data(), sizeof g_tr);
+    std::memcpy(g_tr_key, key, sizeof key);
+    g_tr_valid = true;
 }
 
 __global__ void k_gauss_field(double *__restrict__ src, const double *__restrict__ m,
@@ -180,15 +120,18 @@ extern "C" int ns_step_noalloc(const ns_params *p, double *U, int64_t pitch, int
         (p->source_mode == NS_SRC_GAUSSIAN && (!p->m || !p->n || !(p->r0 != 0.0))) ||
         (p->source_mode == NS_SRC_FIELD && !p->src_field))
         return fail(NS_ERR_PARAM, "ns_step_noalloc: a required setup array is NULL");
-    if (pitch < p->imax || pitch % 32 != 0)
-        return fail(NS_ERR_PARAM, "ns_step_noalloc: pitch=%lld must be >= imax and a multiple of 32",
-                    (long long)pitch);
+    if (pitch < p->imax || pitch % 32 != 0 ||
+        pitch > (int64_t)(NS_NOALLOC_MAX_BYTES / sizeof(double)))
+        return fail(NS_ERR_PARAM,
+                    "ns_step_noalloc: pitch=%lld must be >= imax, a multiple of 32 and at most "
+                    "NS_NOALLOC_MAX_BYTES/8", (long long)pitch);
     if (p->imax > NS_NOALLOC_MAX_LINE || p->jmax > NS_NOALLOC_MAX_LINE)
         return fail(NS_ERR_PARAM, "ns_step_noalloc: imax=%d jmax=%d exceed NS_NOALLOC_MAX_LINE=%d",
                     p->imax, p->jmax, NS_NOALLOC_MAX_LINE);
     const int nk = p->nk;
     const size_t P = (size_t)pitch * p->jmax;
-    const size_t need = 5 * nk * P + ns::AUX_COUNT * P + (p->source_mode ? P : 0) +
+    const size_t trn = p->inviscid ? 0 : (size_t)ns::kTrPieces * ns::kTrStride;
+    const size_t need = 5 * nk * P + ns::AUX_COUNT * P + (p->source_mode ? P : 0) + trn +
                         round32(ns::kCoefStride * (size_t)p->imax) +
                         round32(ns::kCoefStride * (size_t)p->jmax) + 3 * round32(p->imax) +
                         5 * round32(p->jmax) + 64;
@@ -202,6 +145,7 @@ extern "C" int ns_step_noalloc(const ns_params *p, double *U, int64_t pitch, int
     std::lock_guard<std::mutex> lock(g_mu);
     const int dev = p->device;
     if (dev < 0 || dev >= kMaxDevices) return fail(NS_ERR_PARAM, "ns_step_noalloc: device=%d", dev);
+    DeviceGuard keep_device;
     cudaError_t e = cudaSetDevice(dev);
     if (e != cudaSuccess) return fail(NS_ERR_CUDA, "ns_step_noalloc: cudaSetDevice: %s", cudaGetErrorString(e));
     if (!g_work_ptr[dev]) {
@@ -216,6 +160,14 @@ extern "C" int ns_step_noalloc(const ns_params *p, double *U, int64_t pitch, int
         g_work_ptr[dev] = ptr;
     }
     cudaStream_t s = (cudaStream_t)stream;
+    // Every call copies its setup arrays from host memory the library reuses
+    // on the next call, so a captured call would replay stale tables.
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    e = cudaStreamIsCapturing(s, &cap);
+    if (e != cudaSuccess || cap != cudaStreamCaptureStatusNone)
+        return fail(NS_ERR_UNSUPPORTED,
+                    "ns_step_noalloc: the stream is capturing (or its capture status is not "
+                    "available); the call copies host tables that the next call reuses");
 
     // Carve the work area; the context struct only carries pointers here.
     ns_ctx c;
@@ -239,6 +191,7 @@ extern "C" int ns_step_noalloc(const ns_params *p, double *U, int64_t pitch, int
     c.aux = take(ns::AUX_COUNT * P);
     c.Ubase = take(nk * P);
     c.src = p->source_mode ? take(P) : nullptr;
+    c.trtab = trn ? take(trn) : nullptr;
     c.xcoef = take(ns::kCoefStride * (size_t)p->imax);
     c.ycoef = take(ns::kCoefStride * (size_t)p->jmax);
     c.sigx = take(p->imax);
@@ -258,8 +211,12 @@ extern "C" int ns_step_noalloc(const ns_params *p, double *U, int64_t pitch, int
     } while (0)
 
     // setup arrays (host -> work area)
-    fill_coef(g_hx, p->imax, p->dm, p->meshx, p->D, p->metric_mode);
-    fill_coef(g_hy, p->jmax, p->dn, p->meshy, p->D, p->metric_mode);
+    line_table(g_hx, p->imax, p->dm, p->meshx, p->D, p->metric_mode);
+    line_table(g_hy, p->jmax, p->dn, p->meshy, p->D, p->metric_mode);
+    if (c.trtab) {
+        transport_table(p);
+        NA_CUDA(cudaMemcpyAsync(c.trtab, g_tr, sizeof g_tr, cudaMemcpyHostToDevice, s));
+    }
     NA_CUDA(cudaMemcpyAsync(c.xcoef, g_hx, sizeof(double) * ns::kCoefStride * p->imax,
                             cudaMemcpyHostToDevice, s));
     NA_CUDA(cudaMemcpyAsync(c.ycoef, g_hy, sizeof(double) * ns::kCoefStride * p->jmax,
@@ -314,14 +271,14 @@ extern "C" int ns_step_noalloc(const ns_params *p, double *U, int64_t pitch, int
         ph.D_mi_s = p->D_mi - ami0;
         ph.D_k_s = p->D_k - ak0;
     }
-    c.fx = filter_coef(p->sigmaf, kDfbX);
-    c.fy = filter_coef(p->sigmaf, kDfbY);
+    c.fx = filter(p->sigmaf, kDfbX);
+    c.fy = filter(p->sigmaf, kDfbY);
     for (int k = 0; k < 6; k++) {
         c.ct[k] = kCt[k];
         c.alpha[k] = kAlpha[k];
         c.beta[k] = kBeta[k];
     }
-    c.warm = warmup(p->sigmaf);
+    c.warm = warmup(p->sigmaf, std::ldexp(1.0, -60), 36);
     int nsm = 152;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     c.nsm = nsm;

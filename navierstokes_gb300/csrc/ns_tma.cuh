@@ -3,7 +3,8 @@
 // One elected thread of a block issues cp.async.bulk.tensor for the block's
 // halo tile; the mbarrier's transaction count covers its bytes.  Every wait
 // on the barrier is bounded: a thread that gives up sets the context's error
-// word and its block returns (the host reports NS_ERR_TIMEOUT).
+// word, drains the copy for a second bounded period and its block returns
+// (the host reports NS_ERR_TIMEOUT).
 #pragma once
 
 #include "ns_internal.cuh"
@@ -45,7 +46,12 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned 
 }
 
 // Waits for phase `parity` of the barrier at most `limit` polls.
-// False: the wait gave up and `err` is set.
+// False: the wait gave up and `err` is set.  A copy the barrier counts may
+// still be in flight when the wait gives up, and a block that exits while it
+// is would leave it landing in shared memory the SM may have handed to the
+// next block; so after giving up the thread keeps polling for up to `limit`
+// more polls before it returns.  Only a copy that never completes at all
+// outlives its block.
 __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsigned parity,
                                                   int *err, long long limit = kTmaSpinLimit)
 {
@@ -53,6 +59,8 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsig
     while (!mbar_try_wait(bar, parity)) {
         if (++spins > limit) {
             atomicExch(err, 1);
+            for (long long k = 0; k < limit && !mbar_try_wait(bar, parity); k++) {
+            }
             return false;
         }
     }

@@ -172,3 +172,15 @@ def test_filter_sweep_is_sequential(oracle_mod):
     seq = U[j, i, 0] - 0.2 * (np.dot(d[:6], F[j, i - 6:i, 0]) + np.dot(d[6:], U[j, i:i + 7, 0]))
     assert abs(F[j, i, 0] - seq) < 1e-13
     assert abs(F[j, i, 0] - jac) > 1e-6
+
+
+@pytest.mark.parametrize("which", range(13))
+def test_library_tables_equal_the_oracle(oracle_mod, nslib, which):
+    """Every setup path of the library (single grid, batch, no-alloc) takes
+    its DRP, filter and LDDRK tables from one header; those tables equal the
+    oracle's restatement of init.f90, filtering.f90 and rk.f90 bit for bit."""
+    out = np.zeros(16)
+    n = nslib.ns_coef_table(which, out.ctypes.data)
+    ref = oracle_mod.coeffs(which)
+    assert n == len(ref)
+    np.testing.assert_array_equal(out[:n], ref)

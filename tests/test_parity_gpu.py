@@ -115,6 +115,20 @@ def test_navier_stokes_4096x2048_ten_steps(oracle_mod, nslib):
     print("4096x2048 NS, 10 steps, per variable (rel max, rel perturbation):", errs)
 
 
+@pytest.mark.slow
+def test_navier_stokes_4096x2048_200_steps(oracle_mod, nslib):
+    """The benchmark workload over its whole stated run: 4096x2048
+    Navier-Stokes on the stretched grid, 200 steps on the GPU against 200
+    oracle steps on every host core (about two minutes), per variable
+    <= 1e-12 of its scale; the error relative to each perturbation is
+    printed beside it."""
+    c = cases.stretched_ns_case()
+    assert c.steps == 200
+    got, ref = _run_both(oracle_mod, c, c.steps)
+    errs = assert_parity(got, ref, c.Ub, label="Navier-Stokes 4096x2048, 200 steps")
+    print("4096x2048 NS, 200 steps, per variable (rel max, rel perturbation):", errs)
+
+
 def test_rk_euler_dropin_matches_resident(oracle_mod, nslib):
     """ns_rk_euler (host U in, host U out, one step per call) equals the
     resident-state path and the oracle."""

@@ -72,6 +72,31 @@ def test_split32_every_perturbation_fp32(nslib, vortex):
         assert l2 <= 2e-4 and mx <= 5e-4
 
 
+@pytest.mark.slow
+def test_split_4096_squared_1000_steps(nslib):
+    """The split-precision workload at full size: 4096x4096 Euler at M = 0.5,
+    pulse 1e-4 and vortex 1e-3, NS_PREC_SPLIT against the FP64 path on the
+    same GPU; p' relative L2 and max error <= 1e-5 at steps 100, 500 and
+    1000."""
+    from navierstokes_gb300 import Solver
+    c = cases.uniform_flow_case()
+    assert (c.imax, c.jmax, c.steps) == (4096, 4096, 1000)
+    marks = (100, 500, 1000)
+    snaps = {}
+    for prec in (L.NS_PREC_FP64, L.NS_PREC_SPLIT):
+        with Solver(c, precision=prec) as s:
+            s.set_state(c.U0)
+            done = 0
+            for n in marks:
+                s.step(done, n - done)
+                done = n
+                snaps[prec, n] = s.get_state()
+    for n in marks:
+        l2, mx = p_errors(snaps[L.NS_PREC_SPLIT, n], snaps[L.NS_PREC_FP64, n], c.Ub)
+        print(f"4096^2 split, step {n}: p' rel L2 {l2:.2e} max {mx:.2e}")
+        assert l2 <= TOL_PPRIME and mx <= TOL_PPRIME, (n, l2, mx)
+
+
 def test_split_with_source_and_chunked_filters(nslib):
     c = cases.uniform_flow_case(imax=1500, jmax=1100, mach=0.3, pulse_amp=0.0, vortex_eps=0.0,
                                 steps=80)

@@ -58,6 +58,47 @@ def test_noalloc_matches_allocating_step_two_calls(nslib):
     del keep
 
 
+@pytest.mark.gpu
+def test_noalloc_soa_base_flow_on_a_stream_after_a_larger_case(nslib):
+    """An inviscid case whose base flow arrives as planes (NS_LAYOUT_SOA), on
+    a stream of the caller's, run straight after a larger viscous case: the
+    work area still holds that case's arrays, and none of it reaches the
+    result."""
+    import torch
+    from navierstokes_gb300 import Solver
+
+    big = cases.mixing_layer_case(imax=160, jmax=120, D=16, dt=0.01)
+    pb, keep_b = cases.params_from_case(big)
+    pitch_b = (big.imax + 31) // 32 * 32
+    dev_b = torch.zeros((big.nk, big.jmax, pitch_b), dtype=torch.float64, device="cuda:0")
+    dev_b[:, :, :big.imax] = torch.from_numpy(
+        np.ascontiguousarray(np.moveaxis(big.U0, 2, 0))).cuda()
+    torch.cuda.synchronize()
+    assert nslib.ns_step_noalloc(C.byref(pb), C.c_void_p(dev_b.data_ptr()), pitch_b, 0, 2,
+                                 None) == L.NS_OK, L.last_error()
+
+    c = cases.acoustic_pulse_case(imax=80, jmax=70, nk=4, D=10)
+    c.source_mode, c.amplitude, c.wf, c.r0 = L.NS_SRC_GAUSSIAN, 1e-3, 0.4, 3.0
+    nsteps = 5
+    with Solver(c) as s:
+        ref = s.run(c.U0, 2, nsteps)
+    p, keep = cases.params_from_case(c)
+    ub_planes = np.ascontiguousarray(np.moveaxis(c.Ub, 2, 0))   # (nk, jmax, imax)
+    p.Ub = ub_planes.ctypes.data
+    p.ub_layout = L.NS_LAYOUT_SOA
+    pitch = (c.imax + 31) // 32 * 32
+    stream = torch.cuda.Stream()
+    dev = torch.zeros((c.nk, c.jmax, pitch), dtype=torch.float64, device="cuda:0")
+    dev[:, :, :c.imax] = torch.from_numpy(np.ascontiguousarray(np.moveaxis(c.U0, 2, 0))).cuda()
+    torch.cuda.synchronize()
+    rc = nslib.ns_step_noalloc(C.byref(p), C.c_void_p(dev.data_ptr()), pitch, 2, nsteps,
+                               C.c_void_p(stream.cuda_stream))
+    assert rc == L.NS_OK, L.last_error()
+    stream.synchronize()
+    assert_parity(_to_fortran(dev, c), ref, c.Ub, label="no-alloc step, planes, own stream")
+    del keep, keep_b
+
+
 def test_noalloc_rejects_cases_beyond_the_work_area(nslib):
     c = cases.acoustic_pulse_case(imax=1024, jmax=1024, nk=5, D=10)
     p, keep = cases.params_from_case(c)
@@ -65,4 +106,9 @@ def test_noalloc_rejects_cases_beyond_the_work_area(nslib):
     assert rc == L.NS_ERR_PARAM
     msg = L.last_error()
     assert "work area" in msg and "NS_NOALLOC_MAX_BYTES" in msg
+    # a pitch whose plane size would wrap is refused before any arithmetic on it
+    c = cases.acoustic_pulse_case(imax=64, jmax=64, nk=4, D=8)
+    p, keep = cases.params_from_case(c)
+    rc = nslib.ns_step_noalloc(C.byref(p), C.c_void_p(1), 1 << 60, 0, 1, None)
+    assert rc == L.NS_ERR_PARAM and "pitch" in L.last_error()
     del keep
