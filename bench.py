@@ -418,8 +418,9 @@ def adjoint_study(args, local):
     radius 150 cells.  Times the plain FP64 forward (ns_step), the forward
     with the loss (every stage input kept when it fits, --adjoint-k 0; else
     checkpoints) and the reverse pass (stage derivatives or segments
-    recomputed, then the stage adjoints), and checks the control gradient at
-    two controls against central differences h = 1e-7."""
+    recomputed, then the stage adjoints; with checkpoints the recompute of
+    one segment runs beside the reverse of the next), and checks the control
+    gradient at two controls against central differences h = 1e-7."""
     import time
     from navierstokes_gb300 import Solver
     from navierstokes_gb300.adjoint import Adjoint, SourceProblem
@@ -752,8 +753,9 @@ def main():
     ap.add_argument("--cpu-workloads", action="store_true",
                     help="also time the C oracle on every workload (all cores, 1 core)")
     ap.add_argument("--adjoint-steps", type=int, default=2000)
-    ap.add_argument("--adjoint-k", type=int, default=0,
-                    help="adjoint checkpoint interval; 0 keeps every stage input if it fits")
+    ap.add_argument("--adjoint-k", type=int, default=100,
+                    help="adjoint checkpoint interval (the workload's 100); 0 keeps every stage "
+                         "input if it fits")
     ap.add_argument("--split-error-steps", type=lambda t: [int(x) for x in t.split(",")],
                     default=[100, 500, 1000])
     args = ap.parse_args()

@@ -43,7 +43,8 @@ typedef enum ns_status {
     NS_ERR_NONFINITE = 4,   /* the state holds NaN/Inf (ns_check_finite) */
     NS_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up */
     NS_ERR_STATE = 6,       /* call out of order (e.g. step before set_state) */
-    NS_ERR_UNSUPPORTED = 7  /* feature not available for these parameters */
+    NS_ERR_UNSUPPORTED = 7, /* feature not available for these parameters */
+    NS_ERR_CHECK = 8        /* checked build only: a device index check failed */
 } ns_status;
 
 /* Host array layouts accepted by ns_set_state/ns_get_state. */
@@ -248,6 +249,17 @@ NS_API int ns_transport_eval(ns_ctx *ctx, const double *T, double *mu, double *k
  * NS_ERR_TIMEOUT when the wait ran out and reported it, as the stage
  * kernels do (their limit is 2^24 polls). */
 NS_API int ns_tma_wait_test(int device, long long spin_limit);
+
+/* Library diagnostics of the checked build, no counterpart in the reference.
+ * The checked build (libns_gb300_checked.so, compiled with -DNS_CHECKED)
+ * range-checks every tile, halo, segment and work-list index its kernels
+ * derive; a failed check is recorded instead of the access and the next
+ * synchronising call returns NS_ERR_CHECK with the file and line in
+ * ns_last_error.  ns_checked_build() is 1 in that build and 0 otherwise;
+ * ns_check_selftest runs one warp in which half the lanes fail a check that
+ * guards no access: NS_ERR_CHECK in the checked build, NS_OK otherwise. */
+NS_API int ns_checked_build(void);
+NS_API int ns_check_selftest(int device);
 
 /* Library diagnostic, host only: the piecewise-polynomial table of mu(T),
  * k(T) that ns_create builds for a viscous context (Tref, fits {A,B,C,D} of

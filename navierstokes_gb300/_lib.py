@@ -6,9 +6,13 @@ missing or unloadable library raises ImportError naming the build step.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from pathlib import Path
 
-LIB_PATH = Path(__file__).resolve().parent / "libns_gb300.so"
+# NS_GB300_LIB names another build of the same library to load instead (the
+# checked build, libns_gb300_checked.so); it must exist like the default.
+LIB_PATH = Path(os.environ.get("NS_GB300_LIB") or
+                Path(__file__).resolve().parent / "libns_gb300.so").resolve()
 
 NS_OK = 0
 NS_ERR_PARAM = 1
@@ -18,6 +22,7 @@ NS_ERR_NONFINITE = 4
 NS_ERR_TIMEOUT = 5
 NS_ERR_STATE = 6
 NS_ERR_UNSUPPORTED = 7
+NS_ERR_CHECK = 8
 
 NS_LAYOUT_FORTRAN = 0
 NS_LAYOUT_SOA = 1
@@ -62,6 +67,8 @@ SIGNATURES = [
     ("ns_transport_eval", C.c_int, [_VP, _VP, _VP, _VP, C.c_int]),
     ("ns_adjoint_stored_bytes", C.c_int, [_VP, C.POINTER(C.c_int64)]),
     ("ns_tma_wait_test", C.c_int, [C.c_int, C.c_longlong]),
+    ("ns_checked_build", C.c_int, []),
+    ("ns_check_selftest", C.c_int, [C.c_int]),
     ("ns_transport_table", C.c_int, [C.c_double, _VP, _VP, _VP]),
     ("ns_coef_table", C.c_int, [C.c_int, _VP]),
     ("ns_pin_host", C.c_int, [_VP, C.c_size_t]),

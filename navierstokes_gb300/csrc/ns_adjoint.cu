@@ -12,7 +12,12 @@
 // Jacobians (eqeuler.f90:63-92) and the DRP derivatives with their closures
 // and metrics (diff.f90:6-350).  The forward state is checkpointed every K
 // steps; each K-step segment is recomputed once, keeping every stage's input
-// state and derivatives, so the reverse pass recomputes nothing.
+// state and derivatives, so the reverse pass recomputes nothing.  The
+// forward keeps the last segment's stage inputs itself, and the recompute of
+// segment s-1 runs on a second stream beside the reverse of segment s (two
+// segment stores): on grids of a few hundred thousand points one kernel
+// leaves much of the GPU idle, and the two chains are independent.
+#include <algorithm>
 #include <cmath>
 #include <string>
 #include <vector>
@@ -440,7 +445,13 @@ struct ns_adjoint {
     double *loss = nullptr;
     double *chk = nullptr;     // checkpoints: nchk x 4 planes
     int nchk = 0;
-    double *store = nullptr;   // segment: K steps x 6 stages x 12 planes (U, dU/dx, dU/dy)
+    // segment stores: K steps x 6 stages x 12 planes (U, dU/dx, dU/dy), then
+    // 4 planes for the state after the segment's last step; segment sg uses
+    // store2 when sg is odd and store2 exists (recompute beside reverse)
+    double *store = nullptr, *store2 = nullptr;
+    bool last_seg_stored = false;  // the forward kept the last segment's stages
+    cudaStream_t s_rec = nullptr, s_rev = nullptr;
+    cudaEvent_t ev_rec[2] = {}, ev_rev[2] = {}, ev_start = nullptr;
     // K = 0: every stage's input of every step kept (nsteps x 6 x 4 planes)
     // when device memory allows; the reverse pass then recomputes only the
     // first derivatives of each stage instead of the whole forward
@@ -477,6 +488,41 @@ int aerr(ns_adjoint *a, int code, const std::string &m)
         if (e_ != cudaSuccess) return aerr((a), NS_ERR_CUDA, std::string(#call ": ") + cudaGetErrorString(e_)); \
     } while (0)
 
+// Planes of one step in a segment store (6 stages x U, dU/dx, dU/dy).
+constexpr size_t kStepPlanes = 6 * 12;
+
+double *seg_store(const ns_adjoint *a, int sg)
+{
+    return (a->store2 && (sg & 1)) ? a->store2 : a->store;
+}
+
+double *seg_slot(double *store, int q, size_t P) { return store + (size_t)q * kStepPlanes * P; }
+
+// (Re)allocates the segment stores for K steps: the first is required, the
+// second only lets the recompute run beside the reverse pass.
+int ensure_segment_stores(ns_adjoint *a, int K)
+{
+    const size_t P = (size_t)a->fwd->d.plane;
+    const size_t bytes = ((size_t)K * kStepPlanes + 4) * P * sizeof(double);
+    if (a->store_steps < K) {
+        if (a->store) cudaFree(a->store);
+        if (a->store2) cudaFree(a->store2);
+        a->store = a->store2 = nullptr;
+        a->store_steps = 0;
+        A_CUDA(a, cudaMalloc(&a->store, bytes));
+        a->store_steps = K;
+    }
+    if (!a->store2) {
+        size_t freeb = 0, total = 0;
+        const bool room = cudaMemGetInfo(&freeb, &total) == cudaSuccess && bytes <= freeb / 4 * 3;
+        if (!room || cudaMalloc(&a->store2, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            a->store2 = nullptr;
+        }
+    }
+    return NS_OK;
+}
+
 // sin(wf*((iter+c_k)*dt)) of rk.f90:188 for the six stages of step `iter`
 void stage_sines(const ns_ctx *c, int iter, double *out)
 {
@@ -485,11 +531,10 @@ void stage_sines(const ns_ctx *c, int iter, double *out)
 
 // One forward step stage by stage; when `slot` is non-null, each stage's
 // input U and its derivatives are kept there (12 planes per stage).
-int forward_step(ns_adjoint *a, int iter, double *slot)
+int forward_step(ns_adjoint *a, int iter, double *slot, cudaStream_t s)
 {
     ns_ctx *c = a->fwd;
     const size_t P = (size_t)c->d.plane;
-    cudaStream_t s = c->stream;
     int cls[ns::kMaxStepLaunches], stg[ns::kMaxStepLaunches];
     const int n = ns::step_sequence(c, cls, stg);
     A_CUDA(a, ns::launch_set_iter(c->d_iter, iter, s));
@@ -512,11 +557,10 @@ int forward_step(ns_adjoint *a, int iter, double *slot)
 // The reverse of one stage: U, Um, Un are the stage's input state and its
 // first derivatives (4 planes each).
 int stage_adjoint(ns_adjoint *a, const double *U, const double *Um, const double *Un, int stage,
-                  double sink)
+                  double sink, cudaStream_t s)
 {
     ns_ctx *c = a->fwd;
     const ns::Dims &d = c->d;
-    cudaStream_t s = c->stream;
     ns::adj::k_bct_cols<<<(d.imax + 127) / 128, 128, 0, s>>>(a->lam, d);
     ns::adj::k_bct_rows<<<(d.jmax + 127) / 128, 128, 0, s>>>(a->lam, d);
     {
@@ -655,7 +699,7 @@ int ns_adjoint_create(const ns_params *p, int nobs, const double *obs_x, const d
     cudaError_t e = cudaMalloc(&a->obs, nobs * sizeof(ns::adj::Obs));
     if (e == cudaSuccess) e = cudaMalloc(&a->loss, sizeof(double));
     a->store_steps = a->K;
-    const size_t store_planes = a->K ? (size_t)a->K * 6 * 12 : 12;
+    const size_t store_planes = a->K ? (size_t)a->K * kStepPlanes + 4 : 12;
     if (e == cudaSuccess) e = cudaMalloc(&a->store, store_planes * P * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&a->d_step, sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&a->endstate, 4 * P * sizeof(double));
@@ -684,10 +728,14 @@ void ns_adjoint_destroy(ns_adjoint *a)
         a->fwd->dudn = a->dudn0;
     }
     if (a->fwd_exec) cudaGraphExecDestroy(a->fwd_exec);
-    void *ps[] = {a->obs, a->loss, a->chk, a->store, a->endstate, a->lam, a->lam2, a->om,
-                  a->lx, a->ly, a->gS, a->stages, a->d_step};
+    void *ps[] = {a->obs, a->loss, a->chk, a->store, a->store2, a->endstate, a->lam, a->lam2,
+                  a->om, a->lx, a->ly, a->gS, a->stages, a->d_step};
     for (void *p : ps)
         if (p) cudaFree(p);
+    for (cudaStream_t st : {a->s_rec, a->s_rev})
+        if (st) cudaStreamDestroy(st);
+    for (cudaEvent_t ev : {a->ev_rec[0], a->ev_rec[1], a->ev_rev[0], a->ev_rev[1], a->ev_start})
+        if (ev) cudaEventDestroy(ev);
     if (a->fwd) ns_destroy(a->fwd);
     delete a;
 }
@@ -733,14 +781,7 @@ int ns_adjoint_forward(ns_adjoint *a, const double *U0, int layout, int iter0, i
         return NS_OK;
     }
     const int K = a->K ? a->K : kDefaultCheckpoint;
-    if (a->store_steps < K) {
-        // every-stage storage did not fit: segments of K steps
-        if (a->store) cudaFree(a->store);
-        a->store = nullptr;
-        a->store_steps = 0;
-        A_CUDA(a, cudaMalloc(&a->store, (size_t)K * 6 * 12 * P * sizeof(double)));
-        a->store_steps = K;
-    }
+    if ((rc = ensure_segment_stores(a, K)) != NS_OK) return rc;
     const int nchk = (nsteps + K - 1) / K;
     if (nchk > a->nchk) {
         if (a->chk) cudaFree(a->chk);
@@ -748,21 +789,30 @@ int ns_adjoint_forward(ns_adjoint *a, const double *U0, int layout, int iter0, i
         A_CUDA(a, cudaMalloc(&a->chk, (size_t)nchk * 4 * P * sizeof(double)));
         a->nchk = nchk;
     }
+    // the last segment's steps keep their stage inputs and derivatives (the
+    // reverse pass starts there without recomputing it); the rest replay the
+    // step graph
+    const int last0 = (nchk - 1) * K;
+    double *last = seg_store(a, nchk - 1);
     A_CUDA(a, cudaMemsetAsync(a->loss, 0, sizeof(double), s));
     for (int n = 0; n < nsteps; n++) {
         if (n % K == 0)
             A_CUDA(a, cudaMemcpyAsync(a->chk + (size_t)(n / K) * 4 * P, c->U, 4 * P * sizeof(double),
                                       cudaMemcpyDeviceToDevice, s));
-        rc = ns_step(c, iter0 + n, 1);
+        rc = (n >= last0) ? forward_step(a, iter0 + n, seg_slot(last, n - last0, P), s)
+                          : ns_step(c, iter0 + n, 1);
         if (rc != NS_OK) return rc;
         ns::adj::k_obs_loss<<<1, 32, 0, s>>>(c->U, c->d, a->obs, a->nobs, a->pb, a->loss);
     }
+    A_CUDA(a, cudaMemcpyAsync(seg_slot(last, nsteps - last0, P), c->U, 4 * P * sizeof(double),
+                              cudaMemcpyDeviceToDevice, s));
     A_CUDA(a, cudaMemcpyAsync(a->endstate, c->U, 4 * P * sizeof(double), cudaMemcpyDeviceToDevice, s));
     A_CUDA(a, cudaMemcpyAsync(loss, a->loss, sizeof(double), cudaMemcpyDeviceToHost, s));
     if ((rc = ns_synchronize(c)) != NS_OK) return aerr(a, rc, ns_last_error(c));
     a->nsteps = nsteps;
     a->iter0 = iter0;
     a->forward_done = true;
+    a->last_seg_stored = true;
     return NS_OK;
 }
 
@@ -802,38 +852,120 @@ int ns_adjoint_backward(ns_adjoint *a, double *grad_field)
                 c->dudm = a->dudm0;
                 c->dudn = a->dudn0;
                 A_CUDA(a, e);
-                if ((rc = stage_adjoint(a, U, Um, Un, st, sn[st])) != NS_OK) return rc;
+                if ((rc = stage_adjoint(a, U, Um, Un, st, sn[st], s)) != NS_OK) return rc;
             }
         }
     }
     const int K = a->K ? a->K : kDefaultCheckpoint;
     const int nseg = a->stored_all ? 0 : (a->nsteps + K - 1) / K;
-    for (int sg = nseg - 1; sg >= 0; sg--) {
-        const int n0 = sg * K, n1 = std::min(a->nsteps, n0 + K);
-        // recompute the segment, keeping every stage's input and derivatives
+    // Segments: the recompute of segment sg-1 (stream s_rec) runs beside the
+    // reverse of segment sg (stream s_rev) when the second store exists;
+    // events order each store's writer after its previous reader.
+    cudaStream_t srec = s, srev = s;
+    if (nseg > 0) {
+        if (!a->s_rec) {
+            A_CUDA(a, cudaStreamCreateWithFlags(&a->s_rec, cudaStreamNonBlocking));
+            A_CUDA(a, cudaStreamCreateWithFlags(&a->s_rev, cudaStreamNonBlocking));
+            for (int k = 0; k < 2; k++) {
+                A_CUDA(a, cudaEventCreateWithFlags(&a->ev_rec[k], cudaEventDisableTiming));
+                A_CUDA(a, cudaEventCreateWithFlags(&a->ev_rev[k], cudaEventDisableTiming));
+            }
+            A_CUDA(a, cudaEventCreateWithFlags(&a->ev_start, cudaEventDisableTiming));
+        }
+        srec = a->s_rec;
+        srev = a->s_rev;
+        // both start after everything enqueued on the context's stream
+        A_CUDA(a, cudaEventRecord(a->ev_start, s));
+        A_CUDA(a, cudaStreamWaitEvent(srec, a->ev_start, 0));
+        A_CUDA(a, cudaStreamWaitEvent(srev, a->ev_start, 0));
+    }
+    const bool pipe = a->store2 != nullptr;
+    auto seg_n0 = [&](int sg) { return sg * K; };
+    auto seg_len = [&](int sg) { return std::min(a->nsteps, (sg + 1) * K) - sg * K; };
+    // recompute segment sg from its checkpoint, keeping every stage's input
+    // and derivatives, and the state after its last step
+    auto rec_begin = [&](int sg) -> int {
         A_CUDA(a, cudaMemcpyAsync(c->U, a->chk + (size_t)sg * 4 * P, 4 * P * sizeof(double),
-                                  cudaMemcpyDeviceToDevice, s));
-        for (int n = n0; n < n1; n++)
-            if ((rc = forward_step(a, a->iter0 + n, a->store + (size_t)(n - n0) * 6 * 12 * P)) != NS_OK)
-                return rc;
-        for (int n = n1 - 1; n >= n0; n--) {
-            // loss term of U_{n+1}: the state after step n
-            const double *Unext = (n == n1 - 1) ? c->U : a->store + (size_t)(n + 1 - n0) * 6 * 12 * P;
-            ns::adj::k_obs_grad<<<(a->nobs + 63) / 64, 64, 0, s>>>(Unext, d, a->obs, a->nobs, a->pb, a->lam);
-            A_CUDA(a, cudaMemsetAsync(a->om, 0, 4 * P * sizeof(double), s));
-            double sn[6];
-            stage_sines(c, a->iter0 + n, sn);
-            const double *slot = a->store + (size_t)(n - n0) * 6 * 12 * P;
-            for (int st = 5; st >= 0; st--) {
-                const double *U = slot + (size_t)st * 12 * P;
-                if ((rc = stage_adjoint(a, U, U + 4 * P, U + 8 * P, st, sn[st])) != NS_OK)
-                    return rc;
+                                  cudaMemcpyDeviceToDevice, srec));
+        return NS_OK;
+    };
+    auto rec_step = [&](int sg, int q) -> int {
+        return forward_step(a, a->iter0 + seg_n0(sg) + q, seg_slot(seg_store(a, sg), q, P), srec);
+    };
+    auto rec_end = [&](int sg) -> int {
+        A_CUDA(a, cudaMemcpyAsync(seg_slot(seg_store(a, sg), seg_len(sg), P), c->U,
+                                  4 * P * sizeof(double), cudaMemcpyDeviceToDevice, srec));
+        A_CUDA(a, cudaEventRecord(a->ev_rec[sg & 1], srec));
+        return NS_OK;
+    };
+    // reverse of step n of segment sg: the loss term of the state after it,
+    // then its six stages
+    auto rev_step = [&](int sg, int n) -> int {
+        double *st = seg_store(a, sg);
+        const int q = n - seg_n0(sg);
+        ns::adj::k_obs_grad<<<(a->nobs + 63) / 64, 64, 0, srev>>>(seg_slot(st, q + 1, P), d, a->obs,
+                                                                   a->nobs, a->pb, a->lam);
+        A_CUDA(a, cudaMemsetAsync(a->om, 0, 4 * P * sizeof(double), srev));
+        double sn[6];
+        stage_sines(c, a->iter0 + n, sn);
+        const double *slot = seg_slot(st, q, P);
+        for (int k = 5; k >= 0; k--) {
+            const double *U = slot + (size_t)k * 12 * P;
+            const int r = stage_adjoint(a, U, U + 4 * P, U + 8 * P, k, sn[k], srev);
+            if (r != NS_OK) return r;
+        }
+        return NS_OK;
+    };
+#define A_TRY(call)                        \
+    do {                                   \
+        if ((rc = (call)) != NS_OK) return rc; \
+    } while (0)
+    if (nseg > 0) {
+        if (a->last_seg_stored) {
+            A_CUDA(a, cudaEventRecord(a->ev_rec[(nseg - 1) & 1], srec));
+        } else {
+            A_TRY(rec_begin(nseg - 1));
+            for (int q = 0; q < seg_len(nseg - 1); q++) A_TRY(rec_step(nseg - 1, q));
+            A_TRY(rec_end(nseg - 1));
+        }
+    }
+    // the stores are reused below: a second backward recomputes every segment
+    a->last_seg_stored = false;
+    for (int sg = nseg - 1; sg >= 0; sg--) {
+        A_CUDA(a, cudaStreamWaitEvent(srev, a->ev_rec[sg & 1], 0));
+        const int nr = seg_len(sg), n1 = seg_n0(sg) + nr;
+        const int nc = sg > 0 ? seg_len(sg - 1) : 0;
+        if (pipe) {
+            if (sg > 0) {
+                // segment sg-1 goes into the store segment sg+1 was reversed from
+                if (sg + 1 < nseg) A_CUDA(a, cudaStreamWaitEvent(srec, a->ev_rev[(sg + 1) & 1], 0));
+                A_TRY(rec_begin(sg - 1));
+            }
+            // one step of each chain at a time, so that neither stream's
+            // queue runs ahead of the other's
+            for (int q = 0; q < std::max(nr, nc); q++) {
+                if (q < nr) A_TRY(rev_step(sg, n1 - 1 - q));
+                if (q < nc) A_TRY(rec_step(sg - 1, q));
+            }
+            if (sg > 0) A_TRY(rec_end(sg - 1));
+            A_CUDA(a, cudaEventRecord(a->ev_rev[sg & 1], srev));
+        } else {
+            for (int q = 0; q < nr; q++) A_TRY(rev_step(sg, n1 - 1 - q));
+            A_CUDA(a, cudaEventRecord(a->ev_rev[sg & 1], srev));
+            if (sg > 0) {
+                A_CUDA(a, cudaStreamWaitEvent(srec, a->ev_rev[sg & 1], 0));
+                A_TRY(rec_begin(sg - 1));
+                for (int q = 0; q < nc; q++) A_TRY(rec_step(sg - 1, q));
+                A_TRY(rec_end(sg - 1));
             }
         }
     }
+#undef A_TRY
     const size_t row = (size_t)d.imax * sizeof(double);
     A_CUDA(a, cudaMemcpy2DAsync(grad_field, row, a->gS, d.pitch * sizeof(double), row,
-                                (size_t)d.jmax, cudaMemcpyDeviceToHost, s));
+                                (size_t)d.jmax, cudaMemcpyDeviceToHost, srev));
+    A_CUDA(a, cudaStreamSynchronize(srec));
+    A_CUDA(a, cudaStreamSynchronize(srev));
     if ((rc = ns_synchronize(c)) != NS_OK) return aerr(a, rc, ns_last_error(c));
     // leave the context's state at the forward end state
     A_CUDA(a, cudaMemcpy(c->U, a->endstate, 4 * P * sizeof(double), cudaMemcpyDeviceToDevice));

@@ -17,6 +17,7 @@
 #include <cudaTypedefs.h>
 #include <mutex>
 
+#include "ns_check.cuh"
 #include "ns_coef.h"
 #include "ns_internal.cuh"
 
@@ -405,6 +406,18 @@ int create_split(ns_ctx *c)
 }  // namespace
 
 namespace ns {
+int check_error(int word)
+{
+    static const char *const files[] = {"?", "ns_kernels.cu", "ns_split.cu", "ns_batch.cu",
+                                        "ns_adjoint.cu"};
+    const int f = (word >> 16) & 0xff, line = word & 0xffff;
+    char buf[160];
+    snprintf(buf, sizeof buf, "checked build: an index check failed in %s line %d",
+             f < 5 ? files[f] : "?", line);
+    record_error(buf);
+    return NS_ERR_CHECK;
+}
+
 void build_line_coef(std::vector<double> &tab, int n, double h, const double *mesh, int D,
                      int metric_mode)
 {
@@ -876,6 +889,7 @@ static int check_kernel_err(ns_ctx *c)
     if (!h) return NS_OK;
     NS_CUDA(c, cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream));
     NS_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (h & ns::kCheckTag) return ns::check_error(h);
     return set_err(c, NS_ERR_TIMEOUT, "a stage kernel timed out waiting for its TMA tile");
 }
 

@@ -24,6 +24,7 @@
 #include <cstring>
 #include <vector>
 
+#include "ns_check.cuh"
 #include "ns_coef.h"
 #include "ns_internal.cuh"
 
@@ -46,6 +47,7 @@ struct Args {
     const int4 *tiles, *fx, *fy;
     const int *bc;
     int ntiles, nfx, nfy, nbc;
+    int ninst;                 // instances (the bound of every item's .x)
     void *q0, *q1;             // T*
     double *W;
     // tables in the state's precision T (xcl, ycl: FP32 low parts, split only)
@@ -135,7 +137,7 @@ __device__ __forceinline__ bool grid_barrier(const Args &a)
                 while (*(volatile unsigned *)a.bar_gen == g) {
                     if (*(volatile int *)a.err != 0) { ok = 0; break; }
                     if (++spins > a.spin_limit) {
-                        atomicExch(a.err, 1);
+                        atomicCAS(a.err, 0, 1);  // the first failure recorded wins
                         ok = 0;
                         break;
                     }
@@ -201,8 +203,13 @@ __device__ void tile_issue(const Args &a, int4 item, const T *qin, T *sqbuf)
 {
     constexpr int SW = tile_sw<TY>(), SH = tile_sh<TY>();
     T(*sq)[SH][SW] = reinterpret_cast<T(*)[SH][SW]>(sqbuf);
+    NS_CHECK(a.err, kChkBatch, item.x >= 0 && item.x < a.ninst);
     const Inst in = a.inst[item.x];
     const int i0 = item.y, j0 = item.z;
+    // a tile of kTX x TY points inside its instance; 8 warps of 32 lanes
+    NS_CHECK(a.err, kChkBatch, blockDim.x == 32 * kWarps && i0 >= 0 && i0 % kTX == 0 &&
+                                   i0 < in.imax && j0 >= 0 && j0 % TY == 0 && j0 < in.jmax &&
+                                   in.pitch >= in.imax);
     const long long plane = (long long)in.pitch * in.jmax;
     const T *q = qin + in.q_off;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
@@ -233,8 +240,14 @@ __device__ void stage_tile(const Args &a, int st, int4 item, const T *qin, T *qo
 {
     constexpr int SW = tile_sw<TY>(), SH = tile_sh<TY>();
     const T(*sq)[SH][SW] = reinterpret_cast<const T(*)[SH][SW]>(sqbuf);
+    NS_CHECK(a.err, kChkBatch, item.x >= 0 && item.x < a.ninst);
     const Inst in = a.inst[item.x];
     const int i0 = item.y, j0 = item.z;
+    // tile rows ly + kH +- 3 < SH and columns tx + kH +- 3 < SW; closures
+    // need lines of at least 7 points
+    NS_CHECK(a.err, kChkBatch, blockDim.x == 32 * kWarps && TY % kWarps == 0 && i0 >= 0 &&
+                                   i0 < in.imax && j0 >= 0 && j0 < in.jmax && in.imax >= 7 &&
+                                   in.jmax >= 7);
     const long long plane = (long long)in.pitch * in.jmax;
     const T *q = qin + in.q_off;
     T *qo = qout + in.q_off;
@@ -435,8 +448,12 @@ __device__ __forceinline__ FCoef<double> fcoef<double>(const Args &a, int d)
 template <typename T>
 __device__ void fy_item(const Args &a, int4 item, const T *srcq, T *dstq)
 {
+    NS_CHECK(a.err, kChkBatch, item.x >= 0 && item.x < a.ninst);
     const Inst in = a.inst[item.x];
     const int k = item.y, col = item.z + (threadIdx.x & 31), c = item.w;
+    NS_CHECK(a.err, kChkBatch, k >= 0 && k < 4 && item.z >= 0 && item.z % 32 == 0 &&
+                                   item.z < in.imax && c >= 0 && c < in.fy_chunks &&
+                                   in.jmax >= 13);
     if (col >= in.imax) return;
     const int n = in.jmax, chunks = in.fy_chunks, warm = in.warm;
     const long long st = in.pitch;
@@ -448,6 +465,7 @@ __device__ void fy_item(const Args &a, int4 item, const T *srcq, T *dstq)
     const int len2 = n - 12;
     const int a0 = 6 + (int)(((long long)c * len2) / chunks);
     const int b0 = 6 + (int)(((long long)(c + 1) * len2) / chunks);
+    NS_CHECK(a.err, kChkBatch, 6 <= a0 && a0 <= b0 && b0 <= n - 6);
     T w[13];
     int q;
     if (c == 0 || warm < 0 || a0 - warm <= 6) {
@@ -504,11 +522,15 @@ template <typename T, int PW>
 __device__ void fx_item(const Args &a, int4 item, const T *srcq, T *dstq,
                         T (*tbuf)[32][PW + 1])
 {
+    NS_CHECK(a.err, kChkBatch, item.x >= 0 && item.x < a.ninst);
     const Inst in = a.inst[item.x];
     const int lane = threadIdx.x & 31;
     const int k = item.y, row0 = item.z, c = item.w;
     const int n = in.imax, chunks = in.fx_chunks, warm = in.warm;
     const int nrows = min(32, in.jmax - row0);
+    // rows row0 .. row0+nrows-1 (1..32, the tile's rows) of plane k
+    NS_CHECK(a.err, kChkBatch, k >= 0 && k < 4 && row0 >= 0 && row0 % 32 == 0 && nrows >= 1 &&
+                                   c >= 0 && c < chunks && n >= 13 && in.pitch >= n);
     const long long base = in.q_off + (long long)k * in.pitch * in.jmax + (long long)row0 * in.pitch;
     const T *sb = srcq + base;
     T *ob = dstq + base;
@@ -519,6 +541,7 @@ __device__ void fx_item(const Args &a, int4 item, const T *srcq, T *dstq,
     const int b0 = 6 + (int)(((long long)(c + 1) * len2) / chunks);
     const bool exact = (c == 0 || warm < 0 || a0 - warm <= 6);
     const int q0 = exact ? 6 : a0 - warm;
+    NS_CHECK(a.err, kChkBatch, 6 <= a0 && a0 <= b0 && b0 <= n - 6 && q0 >= 6 && q0 <= a0);
     const FCoef<T> fc = fcoef<T>(a, 0);
     // copies of the block starting at step qb (positions qb+7 ..) into tile buf
     auto issue = [&](int buf, int qb) {
@@ -586,6 +609,7 @@ __device__ void fx_item(const Args &a, int4 item, const T *srcq, T *dstq,
 template <typename T>
 __device__ void bc_item(const Args &a, int inst, T *qall)
 {
+    NS_CHECK(a.err, kChkBatch, inst >= 0 && inst < a.ninst);
     const Inst in = a.inst[inst];
     const long long P = (long long)in.pitch * in.jmax;
     T *q = qall + in.q_off;
@@ -973,6 +997,11 @@ int check_err(ns_batch *b)
         cudaMemsetAsync(b->err, 0, sizeof(int), b->stream);
         cudaMemsetAsync(b->bar, 0, 2 * sizeof(unsigned), b->stream);
         cudaStreamSynchronize(b->stream);
+        if (h & ns::kCheckTag) {
+            const int rc = ns::check_error(h);
+            b->err_text = ns_last_error(nullptr);
+            return rc;
+        }
         return berr(b, NS_ERR_TIMEOUT, "ns_batch: a phase barrier of the persistent step kernel timed out");
     }
     return NS_OK;
@@ -1269,6 +1298,7 @@ int ns_batch_create(const ns_params *const *params, int n, int precision, ns_bat
         a.nfx = b->nfx;
         a.nfy = b->nfy;
         a.nbc = b->nbc;
+        a.ninst = b->n;
         a.q0 = b->q[0];
         a.q1 = b->q[1];
         a.W = b->W;

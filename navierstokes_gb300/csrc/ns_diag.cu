@@ -12,6 +12,7 @@
 // threads per SM).  On GB300 the FP64 pipe, not HBM, bounds the FP64 stage
 // kernels, so this is the denominator of their FP64 roofline fraction.
 #include "ns_internal.cuh"
+#include "ns_check.cuh"
 #include "ns_tma.cuh"
 
 namespace {
@@ -123,7 +124,41 @@ __global__ void k_tma_wait_test(int *err, long long limit)
     ns::mbar_wait_bounded(&bar, 0, err, limit);
 }
 
+// One warp: lanes 16..31 fail an index check that guards nothing (no access
+// follows it), so the checked build records it; the ordinary build has no
+// check at all.
+__global__ void k_check_selftest(int *err)
+{
+    NS_CHECK(err, ns::kChkKernels, threadIdx.x < 16);
+}
+
 }  // namespace
+
+extern "C" int ns_checked_build(void)
+{
+#ifdef NS_CHECKED
+    return 1;
+#else
+    return 0;
+#endif
+}
+
+extern "C" int ns_check_selftest(int device)
+{
+    if (cudaSetDevice(device) != cudaSuccess) return NS_ERR_CUDA;
+    int *d = nullptr;
+    if (cudaMalloc(&d, sizeof(int)) != cudaSuccess) return NS_ERR_OOM;
+    int h = 0;
+    cudaError_t e = cudaMemset(d, 0, sizeof(int));
+    if (e == cudaSuccess) {
+        k_check_selftest<<<1, 32>>>(d);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(&h, d, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return NS_ERR_CUDA;
+    return (h & ns::kCheckTag) ? ns::check_error(h) : NS_OK;
+}
 
 extern "C" int ns_tma_wait_test(int device, long long spin_limit)
 {

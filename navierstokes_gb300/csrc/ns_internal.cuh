@@ -253,6 +253,9 @@ cudaError_t launch_rows_to_planes(const double *rows, double *planes, const Dims
 int count_step_launches(const ns_ctx *c);
 // Makes msg the text ns_last_error(NULL) returns (ns_api.cu).
 void record_error(const char *msg);
+// NS_ERR_CHECK for an error word a failed index check of the checked build
+// left (ns_check.cuh), with the file and line as the error text (ns_api.cu).
+int check_error(int word);
 // Split-precision path (ns_split.cu).
 cudaError_t launch_split_kernel(ns_ctx *c, int cls, int stage, cudaStream_t s);
 cudaError_t launch_split_from_full(ns_ctx *c, const double *U, cudaStream_t s);

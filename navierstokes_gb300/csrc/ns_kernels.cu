@@ -23,6 +23,7 @@
 
 #include "ns_fastmath.cuh"
 #include "ns_internal.cuh"
+#include "ns_check.cuh"
 #include "ns_tma.cuh"
 
 namespace ns {
@@ -159,6 +160,11 @@ __global__ void __launch_bounds__(256)
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int i = blockIdx.x * kFirstBX + tx;
     const int j = row0 + blockIdx.y * kFirstBY + ty;
+    // the tile indices below assume this launch shape; the TMA box's x must
+    // be a multiple of 16 bytes (an even number of doubles)
+    NS_CHECK(err, kChkKernels, blockDim.x == kFirstBX && blockDim.y == kFirstBY);
+    NS_CHECK(err, kChkKernels, ((blockIdx.x * kFirstBX - kFirstTileL) & 1) == 0);
+    NS_CHECK(err, kChkKernels, row0 >= 0 && row0 + rows <= d.jmax && d.imax >= 7 && d.jmax >= 7);
     if constexpr (TMA) {
         const bool lead = (tx == 0 && ty == 0);
         if (lead) mbar_init(&tbar, 1);
@@ -255,6 +261,9 @@ __global__ void __launch_bounds__(256)
     const int i = blockIdx.x * kFirstBX + tx;
     const int j = blockIdx.y * kFirstBY + ty;
     const bool lead = (tx == 0 && ty == 0);
+    NS_CHECK(err, kChkKernels, blockDim.x == kFirstBX && blockDim.y == kFirstBY);
+    NS_CHECK(err, kChkKernels, ((blockIdx.x * kFirstBX - kFirstTileL) & 1) == 0);
+    NS_CHECK(err, kChkKernels, d.imax >= 7 && d.jmax >= 7 && d.pitch >= d.imax);
     if constexpr (TMA) {
         if (lead) mbar_init(&tbar, 1);
         __syncthreads();
@@ -458,8 +467,11 @@ __device__ __forceinline__ void shift13(double *w, double v, double next)
 // back to position 6); b == n-6 ends with pass 3.
 __device__ __forceinline__ void filter_piece(const double *__restrict__ s, double *__restrict__ o,
                                              long long st, int n, int a, int b, int warm,
-                                             const FilterCoef &fc)
+                                             const FilterCoef &fc, int *err)
 {
+    // positions read: 0..12 (exact start) or a-warm-6 .. , ahead up to n-1;
+    // written: a .. b-1 and the pass-1/pass-3 ends
+    NS_CHECK(err, kChkKernels, n >= 13 && 6 <= a && a < b && b <= n - 6);
     double w[13];
     int q;
     if (a == 6 || warm < 0 || a - warm <= 6) {
@@ -539,7 +551,7 @@ __device__ __forceinline__ void filter_piece(const double *__restrict__ s, doubl
 template <bool ALONG_Y>
 __global__ void __launch_bounds__(128)
     k_filter(Dims d, const double *__restrict__ src, double *__restrict__ dst, long long seg,
-             int warm, FilterCoef fc)
+             int warm, FilterCoef fc, int *err)
 {
     const int lane = threadIdx.x & 31;
     const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -557,11 +569,14 @@ __global__ void __launch_bounds__(128)
         const long long e = s1 < gend ? s1 : gend;
         const int k = (int)(g / gpk);
         const int line = (int)(g % gpk) * 32 + lane;
+        NS_CHECK(err, kChkKernels, k >= 0 && k < d.nk && sp >= g * len2 && e > sp && e <= gend);
         if (line < nlines) {
             const long long base =
                 (long long)k * d.plane + (ALONG_Y ? line : (long long)line * d.pitch);
+            // the line's last point stays inside plane k
+            NS_CHECK(err, kChkKernels, base + (long long)(n - 1) * st < (long long)(k + 1) * d.plane);
             filter_piece(src + base, dst + base, st, n, 6 + (int)(sp - g * len2),
-                         6 + (int)(e - g * len2), warm, fc);
+                         6 + (int)(e - g * len2), warm, fc, err);
         }
         sp = e;
     }
@@ -818,14 +833,14 @@ static cudaError_t launch_kernel_t(ns_ctx *c, int cls, int stage, cudaStream_t s
         long long seg;
         unsigned nb;
         filter_shape(d.jmax, d.imax, d.nk, c->warm, c->nsm, kFilterWarpsPerSmsp, seg, nb);
-        k_filter<false><<<nb, 128, 0, s>>>(d, c->U, c->U2, seg, c->warm, c->fx);
+        k_filter<false><<<nb, 128, 0, s>>>(d, c->U, c->U2, seg, c->warm, c->fx, c->d_err);
         break;
     }
     case NS_KC_FILTER_Y: {
         long long seg;
         unsigned nb;
         filter_shape(d.imax, d.jmax, d.nk, c->warm, c->nsm, kFilterWarpsPerSmsp, seg, nb);
-        k_filter<true><<<nb, 128, 0, s>>>(d, c->U2, c->U, seg, c->warm, c->fy);
+        k_filter<true><<<nb, 128, 0, s>>>(d, c->U2, c->U, seg, c->warm, c->fy, c->d_err);
         break;
     }
     case NS_KC_BC: {

@@ -26,6 +26,7 @@
 // bit operations (IEEE-754 layouts, round to nearest even): on GB300 the F2F
 // instructions run on the FP64 pipe, which is about 60x slower than FP32.
 #include "ns_internal.cuh"
+#include "ns_check.cuh"
 #include "ns_tma.cuh"
 
 namespace ns {
@@ -195,6 +196,11 @@ __global__ void __launch_bounds__(256, kSplitMinBlocks)
     const int i0 = blockIdx.x * kTX, j0 = blockIdx.y * kTY;
     const long long fplane = (long long)fpitch * d.jmax;
     const bool lead = (tx == 0 && ty == 0);
+    // tile rows ly + kH +- 3 and columns tx + kTL +- 3 stay inside sq for
+    // this launch shape; the box's x times 4 bytes is a multiple of 16
+    NS_CHECK(err, kChkSplit, blockDim.x == kTX && blockDim.y == 8 && kTY % 8 == 0);
+    NS_CHECK(err, kChkSplit, ((i0 - kTL) & 3) == 0 && fpitch >= d.imax && d.imax >= 7 &&
+                                 d.jmax >= 7);
     if (lead) mbar_init(&tbar, 1);
     __syncthreads();
     if (lead) {
@@ -548,7 +554,7 @@ __device__ __forceinline__ void filter_y_line(const float *__restrict__ s,
 template <int NP>
 __global__ void __launch_bounds__(128)
     k_split_filter_y(Dims d, int fpitch, const float *__restrict__ src, float *__restrict__ dst,
-                     int chunks, int warm, FiltF f, const float *__restrict__ corr)
+                     int chunks, int warm, FiltF f, const float *__restrict__ corr, int *err)
 {
     const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long total = (long long)d.imax * 4 * chunks;
@@ -565,6 +571,9 @@ __global__ void __launch_bounds__(128)
     const int b = 6 + (int)(((long long)(c + 1) * len2) / chunks);
     const bool exact = (c == 0 || warm < 0 || a - warm <= 6);
     const int q0 = exact ? 6 : a - warm;
+    // reads q0-6 .. (ahead, guarded) n-1; writes a .. b-1 and the line ends
+    NS_CHECK(err, kChkSplit, k < 4 && c < chunks && n >= 13 && 6 <= a && a <= b && b <= n - 6 &&
+                                 q0 >= 6 && q0 <= a);
     const float *cr = corr + (long long)k * d.jmax;
     if (is_pair<NP>(k))
         filter_y_line<true>(src + base, src + lbase, dst + base, dst + lbase, st, n, a, b, exact,
@@ -718,7 +727,7 @@ __device__ __forceinline__ void filter_x_rows(const float *__restrict__ sbase,
 template <int NP>
 __device__ __forceinline__ void split_filter_x_body(Dims d, int fpitch, const float *__restrict__ src,
                                                     float *__restrict__ dst, int chunks, int warm,
-                                                    const FiltF &f)
+                                                    const FiltF &f, int *err)
 {
     constexpr int kXW = x_warps<NP>();
     constexpr int kXL = NP ? kXW : 1;  // lo tiles only when pairs exist
@@ -742,6 +751,12 @@ __device__ __forceinline__ void split_filter_x_body(Dims d, int fpitch, const fl
     const int b = 6 + (int)(((long long)(c + 1) * len2) / chunks);
     const bool exact = (c == 0 || warm < 0 || a - warm <= 6);
     const int q0 = exact ? 6 : a - warm;
+    // a warp's rows row0 .. row0+nrows-1 (1..32, the tile's rows), its
+    // positions q0-6 .. n-1 (staged copies of positions >= n are zero-size)
+    NS_CHECK(err, kChkSplit, blockDim.x == 32 * kXW && k < 4 && c < chunks && nrows >= 1 &&
+                                 nrows <= 32 && row0 + nrows <= d.jmax);
+    NS_CHECK(err, kChkSplit, n >= 13 && 6 <= a && a <= b && b <= n - 6 && q0 >= 6 && q0 <= a &&
+                                 fpitch >= n);
     if (is_pair<NP>(k))
         filter_x_rows<true>(src + k * fplane + roff, src + (k + 3) * fplane + roff,
                             dst + k * fplane + roff, dst + (k + 3) * fplane + roff, fpitch, n,
@@ -757,16 +772,16 @@ __device__ __forceinline__ void split_filter_x_body(Dims d, int fpitch, const fl
 // minimum (96 registers), the pair variant left to the compiler (111).
 __global__ void __launch_bounds__(32 * x_warps<0>(), 1)
     k_split_filter_x_single(Dims d, int fpitch, const float *__restrict__ src,
-                            float *__restrict__ dst, int chunks, int warm, FiltF f)
+                            float *__restrict__ dst, int chunks, int warm, FiltF f, int *err)
 {
-    split_filter_x_body<0>(d, fpitch, src, dst, chunks, warm, f);
+    split_filter_x_body<0>(d, fpitch, src, dst, chunks, warm, f, err);
 }
 
 __global__ void __launch_bounds__(32 * x_warps<3>())
     k_split_filter_x_pairs(Dims d, int fpitch, const float *__restrict__ src,
-                           float *__restrict__ dst, int chunks, int warm, FiltF f)
+                           float *__restrict__ dst, int chunks, int warm, FiltF f, int *err)
 {
-    split_filter_x_body<3>(d, fpitch, src, dst, chunks, warm, f);
+    split_filter_x_body<3>(d, fpitch, src, dst, chunks, warm, f, err);
 }
 
 // ---------------------------------------------------------------------------
@@ -924,16 +939,16 @@ static cudaError_t launch_split_np(ns_ctx *c, int cls, int stage, cudaStream_t s
         const unsigned nb = (unsigned)((warps + kXW - 1) / kXW);
         if (NP)
             k_split_filter_x_pairs<<<nb, 32 * kXW, 0, s>>>(d, sp.fpitch, qb, qa, sp.fx_chunks,
-                                                           sp.warm, to_f32(c->fx));
+                                                           sp.warm, to_f32(c->fx), c->d_err);
         else
             k_split_filter_x_single<<<nb, 32 * kXW, 0, s>>>(d, sp.fpitch, qb, qa, sp.fx_chunks,
-                                                            sp.warm, to_f32(c->fx));
+                                                            sp.warm, to_f32(c->fx), c->d_err);
         break;
     }
     case NS_KC_SPLIT_FY: {
         const long long t = (long long)d.imax * 4 * sp.fy_chunks;
         k_split_filter_y<NP><<<(unsigned)((t + 127) / 128), 128, 0, s>>>(
-            d, sp.fpitch, qa, qb, sp.fy_chunks, sp.warm, to_f32(c->fy), sp.ycorr);
+            d, sp.fpitch, qa, qb, sp.fy_chunks, sp.warm, to_f32(c->fy), sp.ycorr, c->d_err);
         break;
     }
     case NS_KC_SPLIT_BC: {

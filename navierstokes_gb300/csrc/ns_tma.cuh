@@ -58,7 +58,7 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsig
     long long spins = 0;
     while (!mbar_try_wait(bar, parity)) {
         if (++spins > limit) {
-            atomicExch(err, 1);
+            atomicCAS(err, 0, 1);  // the first failure recorded wins
             for (long long k = 0; k < limit && !mbar_try_wait(bar, parity); k++) {
             }
             return false;

@@ -24,24 +24,32 @@ HERE = Path(__file__).resolve().parent
 SRC = HERE / "ns_oracle.c"
 HDR = HERE / "ns_oracle.h"
 LIB = HERE / "_build" / "libns_oracle.so"
+# The same source built with AddressSanitizer and UndefinedBehaviorSanitizer
+# (abort on the first report); loaded instead of LIB when NS_ORACLE_SANITIZE
+# is set, in a process that preloads the ASan runtime.
+LIB_SANITIZED = HERE / "_build" / "libns_oracle_san.so"
 # -ffp-contract=off: no fused multiply-add, so the oracle rounds every
 # operation as the reference's statements do, on x86 and on Arm alike.
 CFLAGS = ["-O3", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-fno-fast-math",
           "-std=c11", "-Wall"]
+SANITIZE_FLAGS = ["-O1", "-g", "-fno-omit-frame-pointer", "-fsanitize=address,undefined",
+                  "-fno-sanitize-recover=all"]
 
 
-def build(force: bool = False) -> Path:
-    LIB.parent.mkdir(exist_ok=True)
-    if not force and LIB.exists() and LIB.stat().st_mtime >= max(SRC.stat().st_mtime,
+def build(force: bool = False, sanitize: bool = False) -> Path:
+    lib = LIB_SANITIZED if sanitize else LIB
+    lib.parent.mkdir(exist_ok=True)
+    if not force and lib.exists() and lib.stat().st_mtime >= max(SRC.stat().st_mtime,
                                                                   HDR.stat().st_mtime):
-        return LIB
-    tmp = LIB.with_suffix(".tmp.so")
-    cmd = ["gcc", *CFLAGS, str(SRC), "-o", str(tmp), "-lm"]
+        return lib
+    tmp = lib.with_suffix(".tmp.so")
+    flags = [f for f in CFLAGS if f != "-O3"] + SANITIZE_FLAGS if sanitize else CFLAGS
+    cmd = ["gcc", *flags, str(SRC), "-o", str(tmp), "-lm"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{r.stderr}")
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 class OraParams(C.Structure):
@@ -66,7 +74,7 @@ _lib = None
 def lib():
     global _lib
     if _lib is None:
-        path = build()
+        path = build(sanitize=bool(os.environ.get("NS_ORACLE_SANITIZE")))
         L = C.CDLL(str(path))
         L.ora_create.restype = C.c_void_p
         L.ora_create.argtypes = [C.POINTER(OraParams)]
