@@ -319,6 +319,11 @@ NS_API int ns_batch_info(ns_batch *b, int *grid, int *tile_rows, int *blocks_per
  * that do not exist, each wait bounded by spin_limit spins; returns
  * NS_ERR_TIMEOUT and leaves the batch and its state usable. */
 NS_API int ns_batch_barrier_test(ns_batch *b, int extra, long long spin_limit);
+/* Library diagnostic: runs one step (advancing the state, without the graph)
+ * in which block 0 reads the global timer after every phase barrier;
+ * ms[0..3] = the time of phases A (tiles), B (x lines), C (y lines) and
+ * D (edges), each summed over the six stages, barrier waits included. */
+NS_API int ns_batch_phase_times(ns_batch *b, int iter0, double *ms);
 
 /*
  * Discrete adjoint of the FP64 Euler step (inviscid = 1, nk = 4, source

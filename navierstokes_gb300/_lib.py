@@ -85,6 +85,7 @@ SIGNATURES = [
     ("ns_batch_set_stream", C.c_int, [_VP, _VP]),
     ("ns_batch_autotune", C.c_int, [_VP, C.c_int, C.c_int, C.POINTER(C.c_int),
                                     C.POINTER(C.c_int), C.POINTER(C.c_double)]),
+    ("ns_batch_phase_times", C.c_int, [_VP, C.c_int, _VP]),
     ("ns_batch_info", C.c_int, [_VP, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                 C.POINTER(C.c_int), _VP]),
     ("ns_batch_barrier_test", C.c_int, [_VP, C.c_int, C.c_longlong]),

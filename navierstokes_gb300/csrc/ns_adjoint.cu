@@ -94,13 +94,15 @@ __global__ void k_obs_grad(const double *U, Dims d, const Obs *obs, int nobs, do
 // (rows).  An edge value set from 2*q(1) - q(2) sends 2x and -1x of its
 // adjoint inward and is zeroed; a value set to a constant is zeroed.
 // ---------------------------------------------------------------------------
-__global__ void k_bct_cols(double *lam, Dims d)
+// One block: every (column, variable) pair first, then every (row, variable)
+// pair, so that the row transposes see the column transposes' results at the
+// corners as the reverse order requires; the variables are independent.
+__global__ void __launch_bounds__(1024) k_bct(double *lam, Dims d)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= d.imax) return;
     const long long P = d.plane, p = d.pitch;
-    const int jt = d.jmax - 1;
-    for (int k = 0; k < 4; k++) {
+    const int jt = d.jmax - 1, ir = d.imax - 1;
+    for (int e = threadIdx.x; e < 4 * d.imax; e += blockDim.x) {
+        const int k = e / d.imax, i = e % d.imax;
         double *l = lam + k * P + i;
         // bottom^T (cc.f90:55-59)
         const double b = l[0];
@@ -117,16 +119,10 @@ __global__ void k_bct_cols(double *lam, Dims d)
         }
         l[(long long)jt * p] = 0.0;
     }
-}
-
-__global__ void k_bct_rows(double *lam, Dims d)
-{
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= d.jmax) return;
-    const long long P = d.plane;
-    const int ir = d.imax - 1;
-    for (int k = 0; k < 4; k++) {
-        double *l = lam + k * P + (long long)j * d.pitch;
+    __syncthreads();
+    for (int e = threadIdx.x; e < 4 * d.jmax; e += blockDim.x) {
+        const int k = e / d.jmax, j = e % d.jmax;
+        double *l = lam + k * P + (long long)j * p;
         // right^T (cc.f90:32-36)
         const double r = l[ir];
         if (k < 3) {
@@ -561,8 +557,7 @@ int stage_adjoint(ns_adjoint *a, const double *U, const double *Um, const double
 {
     ns_ctx *c = a->fwd;
     const ns::Dims &d = c->d;
-    ns::adj::k_bct_cols<<<(d.imax + 127) / 128, 128, 0, s>>>(a->lam, d);
-    ns::adj::k_bct_rows<<<(d.jmax + 127) / 128, 128, 0, s>>>(a->lam, d);
+    ns::adj::k_bct<<<1, 1024, 0, s>>>(a->lam, d);
     {
         long long seg;
         unsigned nb;

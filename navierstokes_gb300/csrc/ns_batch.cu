@@ -64,6 +64,9 @@ struct Args {
     int *err;
     unsigned nblocks;          // blocks that take part in each barrier
     long long spin_limit;
+    // phase timing (ns_batch_phase_times): block 0 records the global timer
+    // at the start and after every barrier (1 + 6*4 stamps); null otherwise
+    unsigned long long *stamps;
 };
 
 constexpr int kTX = 32, kH = 3, kWarps = 8;
@@ -578,7 +581,7 @@ __device__ void fx_item(const Args &a, int4 item, const T *srcq, T *dstq,
         __syncwarp();
         T(*tb)[PW + 1] = tbuf[buf];
         const int nstep = min(PW, b0 - qb);
-        for (int t = 0; t < nstep; t++) {
+        auto step = [&](int t) {
             const T v = pass2<T>(w, fc.m);
             const T nxt = tb[lane][t];
             tb[lane][t] = v;
@@ -588,6 +591,13 @@ __device__ void fx_item(const Args &a, int4 item, const T *srcq, T *dstq,
 #pragma unroll
             for (int u = 6; u < 12; u++) w[u] = w[u + 1];
             w[12] = nxt;
+        };
+        if (nstep == PW) {
+            // a whole block unrolled: the window slides by register renaming
+#pragma unroll
+            for (int t = 0; t < PW; t++) step(t);
+        } else {
+            for (int t = 0; t < nstep; t++) step(t);
         }
         __syncwarp();
         for (int r = 0; r < nrows; r++)
@@ -681,6 +691,15 @@ __device__ __forceinline__ void for_items(unsigned *ctr, int n, F &&f)
     }
 }
 
+__device__ __forceinline__ void stamp(const Args &a, int slot)
+{
+    if (a.stamps && blockIdx.x == 0 && threadIdx.x == 0) {
+        unsigned long long t;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+        a.stamps[slot] = t;
+    }
+}
+
 template <typename T, int TY>
 __global__ void __launch_bounds__(256) k_batch_step(Args a)
 {
@@ -691,6 +710,7 @@ __global__ void __launch_bounds__(256) k_batch_step(Args a)
     T(*tx2)[32][PW + 1] = reinterpret_cast<T(*)[32][PW + 1]>(smem) + (size_t)warp * 2;
     const long long nwarps = (long long)gridDim.x * kWarps;
     const long long gw = (long long)blockIdx.x * kWarps + warp;
+    stamp(a, 0);
     for (int st = 0; st < 6; st++) {
         T *qa = reinterpret_cast<T *>((st & 1) ? a.q1 : a.q0);
         T *qb = reinterpret_cast<T *>((st & 1) ? a.q0 : a.q1);
@@ -716,13 +736,18 @@ __global__ void __launch_bounds__(256) k_batch_step(Args a)
             }
         }
         if (!grid_barrier(a)) return;
+        stamp(a, 1 + 4 * st);
         for_items(a.work + 2 * st, a.nfx,
                   [&](int wi) { fx_item<T, PW>(a, a.fx[wi], qb, qa, tx2); });
         if (!grid_barrier(a)) return;
+        stamp(a, 2 + 4 * st);
         for_items(a.work + 2 * st + 1, a.nfy, [&](int wi) { fy_item<T>(a, a.fy[wi], qa, qb); });
         if (!grid_barrier(a)) return;
+        stamp(a, 3 + 4 * st);
         for (long long wi = gw; wi < a.nbc; wi += nwarps) bc_item<T>(a, a.bc[wi], qb);
-        if (st < 5 && !grid_barrier(a)) return;
+        if (a.stamps && !grid_barrier(a)) return;  // timed runs close every phase
+        if (!a.stamps && st < 5 && !grid_barrier(a)) return;
+        stamp(a, 4 + 4 * st);
     }
 }
 
@@ -889,9 +914,10 @@ void bfree(ns_batch *b)
 }
 
 template <typename T, int TY>
-cudaError_t launch_step_t(ns_batch *b, cudaStream_t s)
+cudaError_t launch_step_t(ns_batch *b, cudaStream_t s, unsigned long long *stamps)
 {
     ns::batch::Args a = b->args;
+    a.stamps = stamps;
     a.tiles = b->tiles[TY == 8 ? 0 : 1];
     a.ntiles = b->ntiles[TY == 8 ? 0 : 1];
     a.nblocks = (unsigned)b->grid;
@@ -910,7 +936,7 @@ cudaError_t launch_step_t(ns_batch *b, cudaStream_t s)
     return cudaLaunchKernelEx(&cfg, ns::batch::k_batch_step<T, TY>, a);
 }
 
-cudaError_t launch_step(ns_batch *b, cudaStream_t s)
+cudaError_t launch_step(ns_batch *b, cudaStream_t s, unsigned long long *stamps = nullptr)
 {
     // the per-stage item counters start every step at zero
     cudaError_t me = cudaMemsetAsync(b->bar + 2, 0, 12 * sizeof(unsigned), s);
@@ -921,8 +947,10 @@ cudaError_t launch_step(ns_batch *b, cudaStream_t s)
         if (e != cudaSuccess) return e;
     }
     if (b->precision == NS_PREC_SPLIT32)
-        return b->ty == 8 ? launch_step_t<float, 8>(b, s) : launch_step_t<float, 16>(b, s);
-    return b->ty == 8 ? launch_step_t<double, 8>(b, s) : launch_step_t<double, 16>(b, s);
+        return b->ty == 8 ? launch_step_t<float, 8>(b, s, stamps)
+                          : launch_step_t<float, 16>(b, s, stamps);
+    return b->ty == 8 ? launch_step_t<double, 8>(b, s, stamps)
+                      : launch_step_t<double, 16>(b, s, stamps);
 }
 
 size_t smem_for(int precision, int ty)
@@ -1455,6 +1483,37 @@ int ns_batch_step(ns_batch *b, int iter0, int nsteps)
         if (e != cudaSuccess)
             return berr(b, NS_ERR_CUDA, std::string("ns_batch_step: ") + cudaGetErrorString(e));
     }
+    return NS_OK;
+}
+
+// One step (advancing the state, launched directly) with the phase stamps on:
+// ms[0..3] = the time of phases A..D summed over the six stages, each from
+// the barrier before it to the barrier after it (barrier cost included).
+int ns_batch_phase_times(ns_batch *b, int iter0, double *ms)
+{
+    if (!b || !ms) return berr(b, NS_ERR_PARAM, "ns_batch_phase_times: NULL argument");
+    if (!b->have_state) return berr(b, NS_ERR_STATE, "ns_batch_phase_times before ns_batch_set_state");
+    cudaSetDevice(b->dev);
+    constexpr int kStamps = 1 + 6 * 4;
+    unsigned long long *d = nullptr, h[kStamps] = {};
+    if (cudaMalloc(&d, sizeof h) != cudaSuccess) return berr(b, NS_ERR_OOM, "ns_batch_phase_times");
+    cudaError_t e = cudaMemsetAsync(d, 0, sizeof h, b->stream);
+    if (e == cudaSuccess && b->has_src) {
+        ns::batch::k_batch_set_iter<<<1, 1, 0, b->stream>>>(b->d_iter, iter0);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = launch_step(b, b->stream, d);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, d, sizeof h, cudaMemcpyDeviceToHost, b->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    cudaFree(d);
+    if (e != cudaSuccess)
+        return berr(b, NS_ERR_CUDA, std::string("ns_batch_phase_times: ") + cudaGetErrorString(e));
+    const int rc = check_err(b);
+    if (rc != NS_OK) return rc;
+    for (int p = 0; p < 4; p++) ms[p] = 0.0;
+    for (int st = 0; st < 6; st++)
+        for (int p = 0; p < 4; p++)
+            ms[p] += (double)(h[1 + 4 * st + p] - h[4 * st + p]) * 1e-6;
     return NS_OK;
 }
 

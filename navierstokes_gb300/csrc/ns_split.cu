@@ -675,7 +675,8 @@ __device__ __forceinline__ void filter_x_rows(const float *__restrict__ sbase,
         const int nstep = min(32, b - qb);
         float(*tb)[33] = ti[buf];
         float(*tbl)[33] = til[PAIR ? buf : 0];
-        for (int t = 0; t < nstep; t++) {
+        // one step: output q into the tile column it read, window slides
+        auto step = [&](int t) {
             float vh, vl = 0.f;
             if (PAIR) pass2_p(wh, wl, f, vh, vl);
             else vh = pass2_f(wh, f);
@@ -697,6 +698,14 @@ __device__ __forceinline__ void filter_x_rows(const float *__restrict__ sbase,
             }
             wh[12] = nh;
             wl[12] = nl;
+        };
+        if (nstep == 32) {
+            // a whole block unrolled: the window slides by register renaming
+            // instead of 26 moves per step, and the tile columns are constants
+#pragma unroll
+            for (int t = 0; t < 32; t++) step(t);
+        } else {
+            for (int t = 0; t < nstep; t++) step(t);
         }
         __syncwarp();
         // write outputs q = qb .. qb+nstep-1 that this chunk owns (q >= a)

@@ -190,6 +190,13 @@ class Batch:
                                             C.byref(ms)))
         return ty.value, bps.value, ms.value
 
+    def phase_times(self, iter0: int = 0):
+        """Advances one step with the phase stamps on: ms of phases A..D
+        (tiles, x lines, y lines, edges) summed over the six stages."""
+        ms = (C.c_double * 4)()
+        self._rc(self.lib.ns_batch_phase_times(self._h, iter0, ms))
+        return dict(zip(("tiles", "x_lines", "y_lines", "edges"), list(ms)))
+
     def info(self):
         g, ty, bps = C.c_int(), C.c_int(), C.c_int()
         items = (C.c_int * 4)()

@@ -35,6 +35,22 @@ def test_batch_fp64_matches_single_grid(oracle_mod, nslib):
         assert_parity(got[q], ref, c.Ub, label=f"batch fp64 instance {q} {c.imax}x{c.jmax}")
 
 
+def test_single_instance_pulse_201x201_500_steps(oracle_mod, nslib):
+    """The 201x201 Euler pulse (nk = 4) as a batch of one: every step one
+    persistent launch, 500 steps against the oracle."""
+    from navierstokes_gb300 import Batch
+    c = cases.acoustic_pulse_case(nk=4)
+    with Batch([c], precision=L.NS_PREC_FP64) as b:
+        b.set_initial()
+        b.step(0, 500)
+        b.synchronize()
+        got = b.get_state(0)
+    ref = c.U0.copy()
+    oracle_mod.Oracle(c).run(ref, 0, 500)
+    errs = assert_parity(got, ref, c.Ub, label="pulse 201x201 as one persistent instance")
+    print("201x201 batch of one, 500 steps (rel max, rel perturbation):", errs)
+
+
 def test_batch_split_matches_single_split(nslib):
     from navierstokes_gb300 import Batch
     cs = small_sweep(n=4, seed=5)
@@ -61,6 +77,25 @@ def test_batch_autotune_and_info(nslib):
         info = b.info()
         assert info["tile_rows"] == ty and info["items"][3] == len(cs)
         b.synchronize()
+
+
+def test_batch_phase_times(nslib):
+    """The phase stamps of one step: every phase takes time, and together
+    they make up about one step."""
+    import time
+    from navierstokes_gb300 import Batch
+    cs = small_sweep(n=4, seed=11)
+    with Batch(cs, precision=L.NS_PREC_FP64) as b:
+        b.set_initial()
+        b.step(0, 2)
+        b.synchronize()
+        ph = b.phase_times(2)
+        t0 = time.perf_counter()
+        b.step(3, 10)
+        b.synchronize()
+        step_ms = (time.perf_counter() - t0) * 100.0
+    assert all(v > 0 for v in ph.values()), ph
+    assert 0.3 * step_ms < sum(ph.values()) < 3.0 * step_ms, (ph, step_ms)
 
 
 def test_batch_barrier_timeout_is_reported_and_recoverable(nslib):
