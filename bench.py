@@ -226,14 +226,16 @@ def run_reference(args, world, rank):
 
 
 # Algorithmic HBM bytes per point of one launch of the split-precision
-# kernels: q' is 7 FP32 planes (rho'; u', v', p' hi; their lo parts) = 28 B;
-# the stage reads q' and w (4 x FP64) and writes both; each filter reads and
-# writes q'.
-SPLIT_BYTES_PER_POINT = {"k_split_stage": 120, "k_split_filter_x": 56,
+# kernels, averaged over the six stages: q' is 7 FP32 planes (rho'; u', v',
+# p' hi; their lo parts) = 28 B; the stage reads q' and w (4 x FP64) and
+# writes both, except that stage 0 does not read w and stage 5 does not
+# write it (28 + 32 + 28 + 32 = 120 B, minus 32 B in two of six launches);
+# each filter reads and writes q'.
+SPLIT_BYTES_PER_POINT = {"k_split_stage": (6 * 120 - 2 * 32) / 6, "k_split_filter_x": 56,
                          "k_split_filter_y": 56}
-SPLIT_STEP_BYTES_MIN = 1392   # per point-step: 6 x (120 + 2 x 56)
+SPLIT_STEP_BYTES_MIN = 6 * 120 - 2 * 32 + 12 * 56   # 1328 per point-step
 # NS_PREC_SPLIT32: q' is 4 FP32 planes (16 B)
-SPLIT32_BYTES_PER_POINT = {"k_split_stage": 96, "k_split_filter_x": 32,
+SPLIT32_BYTES_PER_POINT = {"k_split_stage": (6 * 96 - 2 * 32) / 6, "k_split_filter_x": 32,
                            "k_split_filter_y": 32}
 
 
@@ -325,7 +327,8 @@ def split_study(args, local, hbm_peak):
                              "achieved": kernels[dom].get("achieved_gbs"),
                              "peak": hbm_peak, "unit": "GB/s",
                              "frac": kernels[dom].get("hbm_frac"),
-                             "step_frac_of_1392B_per_point": step_gbs / hbm_peak},
+                             "step_bytes_per_point": SPLIT_STEP_BYTES_MIN,
+                             "step_frac": step_gbs / hbm_peak},
                 "kernels": kernels,
                 "split32": {"what": "every perturbation one FP32 number (NS_PREC_SPLIT32)",
                             "value": rates["split32"]["value"], "unit": UNIT,
@@ -333,6 +336,45 @@ def split_study(args, local, hbm_peak):
                             "speedup_vs_fp64": rates["split32"]["value"] / rates["fp64"]["value"],
                             "p_error_vs_fp64": p_errors("split32"),
                             "kernels": rates["split32"].get("kernels")}})
+    return out
+
+
+def split_ns_study(args, local, hbm_peak):
+    """The Navier-Stokes workload (4096x2048, y-stretched, M = 0.5, Re = 1000,
+    pulse 1e-3 and vortex 0.1) in split precision against plain FP64: both
+    run its 200 steps from the same start; throughput of each and the p'
+    error at the end."""
+    import torch
+    from navierstokes_gb300 import Solver, cases
+    from navierstokes_gb300 import _lib as L
+    case = build_case(args)
+    nsteps = args.split_ns_steps
+    stream = torch.cuda.Stream()
+    out = {"workload": f"Navier-Stokes {case.imax}x{case.jmax} (the main line's flow), "
+                       f"{nsteps} steps", "unit": UNIT}
+    finals = {}
+    for name, prec in (("fp64", L.NS_PREC_FP64), ("split", L.NS_PREC_SPLIT)):
+        with Solver(case, device=local, precision=prec) as s:
+            s.set_stream(stream.cuda_stream)
+            s.set_state(case.U0)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            s.step(0, nsteps)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / nsteps
+            finals[name] = s.get_state()
+            out[name] = {"value": case.points / (ms * 1e-3) / 1e6, "ms_per_step": ms,
+                         "launches_per_step": s.launches_per_step()}
+    dp = finals["split"][..., 3] - finals["fp64"][..., 3]
+    pr = finals["fp64"][..., 3] - case.Ub[..., 3]
+    out["value"] = out["split"]["value"]
+    out["speedup_vs_fp64"] = out["split"]["value"] / out["fp64"]["value"]
+    out["p_error_vs_fp64"] = {"p_rel_l2": float(np.linalg.norm(dp) / np.linalg.norm(pr)),
+                              "p_rel_max": float(np.max(np.abs(dp)) / np.max(np.abs(pr))),
+                              "at_step": nsteps}
     return out
 
 
@@ -700,6 +742,13 @@ def run_ours(args, world, rank, local, pg):
         except Exception as e:
             split = {"failed": str(e)}
 
+    split_ns = None
+    if rank == 0 and world == 1 and not args.no_split:
+        try:
+            split_ns = split_ns_study(args, local, hbm_peak)
+        except Exception as e:
+            split_ns = {"failed": str(e)}
+
     small = None
     if rank == 0 and world == 1 and not args.no_small_grid:
         try:
@@ -753,6 +802,8 @@ def run_ours(args, world, rank, local, pg):
             line["cpu_baseline"] = cpu
         if split is not None:
             line["split_precision"] = split
+        if split_ns is not None:
+            line["split_precision_ns"] = split_ns
         if small is not None:
             line["small_grid"] = small
         if batched is not None:
@@ -777,6 +828,8 @@ def main():
     ap.add_argument("--no-split", action="store_true",
                     help="skip the split-precision study (Euler 4096^2)")
     ap.add_argument("--split-n", type=int, default=4096)
+    ap.add_argument("--split-ns-steps", type=int, default=200,
+                    help="steps of the Navier-Stokes split-precision comparison")
     ap.add_argument("--no-small-grid", action="store_true",
                     help="skip the 201x201 Euler pulse timing")
     ap.add_argument("--no-batch", action="store_true",

@@ -213,7 +213,10 @@ enum {
     NS_KC_SPLIT_FX = 8,  /* split precision: lddfilterx on the FP32 perturbation */
     NS_KC_SPLIT_FY = 9,  /* split precision: lddfiltery on the FP32 perturbation */
     NS_KC_SPLIT_BC = 10, /* split precision: ccpml on the perturbation */
-    NS_KC_COUNT = 11
+    NS_KC_SPLIT_VISC = 11, /* split precision, Navier-Stokes: tau' and k grad T'
+                              of the perturbation (eqeuler.f90:28-47,
+                              derivs.f90:48-56) */
+    NS_KC_COUNT = 12
 };
 
 /* Advances the state by `reps` steps from iter0, launching every kernel on

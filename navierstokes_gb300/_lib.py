@@ -113,7 +113,7 @@ SIGNATURES = [
 NS_RUN_NO_CONTORNO = 1
 NS_RUN_QUIET = 2
 
-NS_KC_COUNT = 11
+NS_KC_COUNT = 12
 
 
 class NsParams(C.Structure):

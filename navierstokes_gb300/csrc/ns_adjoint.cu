@@ -94,49 +94,79 @@ __global__ void k_obs_grad(const double *U, Dims d, const Obs *obs, int nobs, do
 // (rows).  An edge value set from 2*q(1) - q(2) sends 2x and -1x of its
 // adjoint inward and is zeroed; a value set to a constant is zeroed.
 // ---------------------------------------------------------------------------
-// One block: every (column, variable) pair first, then every (row, variable)
-// pair, so that the row transposes see the column transposes' results at the
-// corners as the reverse order requires; the variables are independent.
-__global__ void __launch_bounds__(1024) k_bct(double *lam, Dims d)
+// Column part (bottom^T, top^T) of column i and row part (right^T, left^T)
+// of row j for variable k.
+__device__ __forceinline__ void bct_col(double *lam, const Dims &d, int k, int i)
 {
-    const long long P = d.plane, p = d.pitch;
-    const int jt = d.jmax - 1, ir = d.imax - 1;
-    for (int e = threadIdx.x; e < 4 * d.imax; e += blockDim.x) {
-        const int k = e / d.imax, i = e % d.imax;
-        double *l = lam + k * P + i;
-        // bottom^T (cc.f90:55-59)
-        const double b = l[0];
-        if (k < 3) {
-            l[p] += 2.0 * b;
-            l[2 * p] -= b;
-        }
-        l[0] = 0.0;
-        // top^T (cc.f90:39-43)
-        const double t = l[(long long)jt * p];
-        if (k < 3) {
-            l[(long long)(jt - 1) * p] += 2.0 * t;
-            l[(long long)(jt - 2) * p] -= t;
-        }
-        l[(long long)jt * p] = 0.0;
+    const long long p = d.pitch;
+    const int jt = d.jmax - 1;
+    double *l = lam + k * d.plane + i;
+    // bottom^T (cc.f90:55-59)
+    const double b = l[0];
+    if (k < 3) {
+        l[p] += 2.0 * b;
+        l[2 * p] -= b;
     }
-    __syncthreads();
-    for (int e = threadIdx.x; e < 4 * d.jmax; e += blockDim.x) {
-        const int k = e / d.jmax, j = e % d.jmax;
-        double *l = lam + k * P + (long long)j * p;
-        // right^T (cc.f90:32-36)
-        const double r = l[ir];
-        if (k < 3) {
-            l[ir - 1] += 2.0 * r;
-            l[ir - 2] -= r;
+    l[0] = 0.0;
+    // top^T (cc.f90:39-43)
+    const double t = l[(long long)jt * p];
+    if (k < 3) {
+        l[(long long)(jt - 1) * p] += 2.0 * t;
+        l[(long long)(jt - 2) * p] -= t;
+    }
+    l[(long long)jt * p] = 0.0;
+}
+
+__device__ __forceinline__ void bct_row(double *lam, const Dims &d, int k, int j)
+{
+    const int ir = d.imax - 1;
+    double *l = lam + k * d.plane + (long long)j * d.pitch;
+    // right^T (cc.f90:32-36)
+    const double r = l[ir];
+    if (k < 3) {
+        l[ir - 1] += 2.0 * r;
+        l[ir - 2] -= r;
+    }
+    l[ir] = 0.0;
+    // left^T (cc.f90:23-27): only u is extrapolated
+    const double a = l[0];
+    if (k == 1) {
+        l[1] += 2.0 * a;
+        l[2] -= a;
+    }
+    l[0] = 0.0;
+}
+
+// The column parts must precede the row parts only where both touch a
+// point: the three columns and rows next to each corner.  Block 0 does the
+// six corner columns, then (after a block barrier) the six corner rows;
+// the other blocks take every other column and row, which touch disjoint
+// points, all at once.  Each (line, variable) pair is one thread.
+__global__ void __launch_bounds__(256) k_bct(double *lam, Dims d)
+{
+    const int ir = d.imax - 1, jt = d.jmax - 1;
+    if (blockIdx.x == 0) {
+        const int t = threadIdx.x;
+        if (t < 24) {
+            const int k = t / 6, c = t % 6;
+            bct_col(lam, d, k, c < 3 ? c : ir - (c - 3));
         }
-        l[ir] = 0.0;
-        // left^T (cc.f90:23-27): only u is extrapolated
-        const double a = l[0];
-        if (k == 1) {
-            l[1] += 2.0 * a;
-            l[2] -= a;
+        __syncthreads();
+        if (t < 24) {
+            const int k = t / 6, c = t % 6;
+            bct_row(lam, d, k, c < 3 ? c : jt - (c - 3));
         }
-        l[0] = 0.0;
+        return;
+    }
+    const int ncol = d.imax - 6, nrow = d.jmax - 6;
+    const long long total = 4LL * (ncol + nrow);
+    for (long long e = (long long)(blockIdx.x - 1) * blockDim.x + threadIdx.x; e < total;
+         e += (long long)(gridDim.x - 1) * blockDim.x) {
+        if (e < 4LL * ncol) bct_col(lam, d, (int)(e / ncol), 3 + (int)(e % ncol));
+        else {
+            const long long r = e - 4LL * ncol;
+            bct_row(lam, d, (int)(r / nrow), 3 + (int)(r % nrow));
+        }
     }
 }
 
@@ -557,7 +587,10 @@ int stage_adjoint(ns_adjoint *a, const double *U, const double *Um, const double
 {
     ns_ctx *c = a->fwd;
     const ns::Dims &d = c->d;
-    ns::adj::k_bct<<<1, 1024, 0, s>>>(a->lam, d);
+    {
+        const long long items = 4LL * (d.imax + d.jmax - 12);
+        ns::adj::k_bct<<<1 + (unsigned)((items + 255) / 256), 256, 0, s>>>(a->lam, d);
+    }
     {
         long long seg;
         unsigned nb;

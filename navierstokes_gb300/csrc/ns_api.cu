@@ -119,7 +119,7 @@ void free_all(ns_ctx *c)
     {
         ns::SplitState &sp = c->sp;
         float *fb[] = {sp.q[0], sp.q[1], sp.xc, sp.yc, sp.xcl, sp.ycl, sp.sigx, sp.sigy, sp.src,
-                       sp.rho_bc, sp.ycorr, sp.mean_buf};
+                       sp.rho_bc, sp.ycorr, sp.mean_buf, sp.tau, sp.trf};
         for (float *b : fb)
             if (b) cudaFree(b);
     }
@@ -162,10 +162,9 @@ int validate(const ns_params *p)
     if (p->precision != NS_PREC_FP64 && p->precision != NS_PREC_SPLIT &&
         p->precision != NS_PREC_SPLIT32)
         return set_err(nullptr, NS_ERR_UNSUPPORTED, "precision=%d is not available", p->precision);
-    if (p->precision != NS_PREC_FP64 && (!p->inviscid || p->nk != 4))
+    if (p->precision != NS_PREC_FP64 && p->nk != 4)
         return set_err(nullptr, NS_ERR_UNSUPPORTED,
-                       "split precision is implemented for the Euler equations (inviscid=1) "
-                       "with nk=4; got inviscid=%d nk=%d", p->inviscid, p->nk);
+                       "split precision carries rho, u, v, p (nk=4); got nk=%d", p->nk);
     if (p->source_mode < NS_SRC_NONE || p->source_mode > NS_SRC_FIELD)
         return set_err(nullptr, NS_ERR_PARAM, "source_mode=%d", p->source_mode);
     if (!(p->dt > 0) || !(p->dm > 0) || !(p->dn > 0) || !(p->gamma > 1.0))
@@ -310,6 +309,13 @@ int create_split(ns_ctx *c)
                                "split precision needs a base flow uniform in x with v = 0 and "
                                "uniform p (violated at i=%d j=%d)", i + 1, j + 1);
         }
+        // viscous: the base flow must be uniform in y as well, so that its own
+        // stresses and heat flux vanish and those of the flow are
+        // perturbation-sized
+        if (c->visc && (rho[j] != rho[0] || uu[j] != uu[0]))
+            return set_err(c, NS_ERR_UNSUPPORTED,
+                           "split precision for Navier-Stokes needs a uniform base flow "
+                           "(rho and u vary in y at j=%d)", j + 1);
     }
     sp.fpitch = (imax + 31) / 32 * 32;
     const size_t P = (size_t)d.plane, FP = (size_t)sp.fpitch * jmax;
@@ -332,6 +338,24 @@ int create_split(ns_ctx *c)
     if ((rc = make_split_map(c, &sp.qmap[0], sp.q[0], 4 + sp.np)) ||
         (rc = make_split_map(c, &sp.qmap[1], sp.q[1], 4 + sp.np)))
         return rc;
+    if (c->visc) {
+        // tau', k grad T' planes and the FP32 transport table
+        if ((rc = dalloc(c, &sp.tau, 5 * FP)) ||
+            (rc = dalloc(c, &sp.trf, (size_t)ns::kTrPieces * ns::kTrStride)) ||
+            (rc = make_split_map(c, &sp.vmap, sp.tau, 5)))
+            return rc;
+        std::vector<double> tab;
+        const double ami[4] = {p->A_mi, p->B_mi, p->C_mi, p->D_mi};
+        const double ak[4] = {p->A_k, p->B_k, p->C_k, p->D_k};
+        ns::build_transport_table(tab, p->Tref, ami, ak);
+        std::vector<float> tabf(tab.begin(), tab.end());
+        if ((rc = upload_vec(c, sp.trf, tabf))) return rc;
+        const cudaError_t me = cudaMemsetAsync(sp.tau, 0, 5 * FP * sizeof(float), c->stream);
+        if (me != cudaSuccess) return cuda_err(c, me, "cudaMemset");
+        // upload_vec's host vector must outlive the copy
+        const cudaError_t se = cudaStreamSynchronize(c->stream);
+        if (se != cudaSuccess) return cuda_err(c, se, "split setup");
+    }
     cudaError_t e = cudaMemsetAsync(sp.q[0], 0, (4 + sp.np) * FP * sizeof(float), c->stream);
     if (e == cudaSuccess)
         e = cudaMemsetAsync(sp.q[1], 0, (4 + sp.np) * FP * sizeof(float), c->stream);
@@ -400,12 +424,38 @@ int create_split(ns_ctx *c)
     sp.mean.p = (float)pb;
     sp.mean.gamma = (float)p->gamma;
     sp.p_bc = 1.0 / p->gamma - pb;
+    if (c->visc) {
+        // GET_COEFFICIENTS (coefficients.f90:78-79): 1/mu0 and 1/k0 folded into
+        // the constant term of the exp/log form
+        const double Tr = p->Tref;
+        const double ami0 = p->A_mi * std::log(Tr) + p->B_mi / Tr + p->C_mi / Tr / Tr + p->D_mi;
+        const double ak0 = p->A_k * std::log(Tr) + p->B_k / Tr + p->C_k / Tr / Tr + p->D_k;
+        ns::SplitVisc &v = sp.vis;
+        v.rho_b = (float)rho[0];
+        v.p_b = (float)pb;
+        v.gamma = (float)p->gamma;
+        v.T_b = (float)(p->gamma * pb / rho[0]);
+        v.inv_re = (float)(1.0 / p->Re);
+        v.gm1_re = (float)((p->gamma - 1.0) / p->Re);
+        v.inv_re_pr = (float)(1.0 / p->Re / p->Pr);
+        v.Tref = (float)Tr;
+        v.A_mi = (float)p->A_mi;
+        v.B_mi = (float)p->B_mi;
+        v.C_mi = (float)p->C_mi;
+        v.D_mi_s = (float)(p->D_mi - ami0);
+        v.A_k = (float)p->A_k;
+        v.B_k = (float)p->B_k;
+        v.C_k = (float)p->C_k;
+        v.D_k_s = (float)(p->D_k - ak0);
+    }
     return NS_OK;
 }
 
 }  // namespace
 
 namespace ns {
+PFN_cuTensorMapEncodeTiled_v12000 tensor_encoder() { return tensor_map_encoder(); }
+
 int check_error(int word)
 {
     static const char *const files[] = {"?", "ns_kernels.cu", "ns_split.cu", "ns_batch.cu",
@@ -1134,7 +1184,7 @@ const char *ns_kernel_name(int k)
     static const char *names[NS_KC_COUNT] = {
         "k_stage_sin",   "k_prim",          "k_first",          "k_update",
         "k_filter_x",    "k_filter_y",      "k_bc",             "k_split_stage",
-        "k_split_filter_x", "k_split_filter_y", "k_split_bc"};
+        "k_split_filter_x", "k_split_filter_y", "k_split_bc", "k_split_visc"};
     return (k >= 0 && k < NS_KC_COUNT) ? names[k] : "";
 }
 

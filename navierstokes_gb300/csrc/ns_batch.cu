@@ -27,6 +27,7 @@
 #include "ns_check.cuh"
 #include "ns_coef.h"
 #include "ns_internal.cuh"
+#include "ns_tma.cuh"
 
 namespace ns {
 namespace batch {
@@ -45,9 +46,12 @@ struct Inst {
 struct Args {
     const Inst *inst;
     const int4 *tiles, *fx, *fy;
-    const int *bc;
+    const int2 *bc;            // edge items: (instance, first of 32 positions)
+    // TMA maps of every instance's halo tile: [(ty16 * n + inst) * 2 + buf],
+    // buf 0 for q0 and 1 for q1; box 40 x (TY + 6) x 4 planes
     int ntiles, nfx, nfy, nbc;
     int ninst;                 // instances (the bound of every item's .x)
+    const CUtensorMap *qmaps;
     void *q0, *q1;             // T*
     double *W;
     // tables in the state's precision T (xcl, ycl: FP32 low parts, split only)
@@ -69,7 +73,10 @@ struct Args {
     unsigned long long *stamps;
 };
 
-constexpr int kTX = 32, kH = 3, kWarps = 8;
+// Tiles of kTX x TY points; their halo box spans kTL columns to the left
+// (the TMA box's x times the element size must be a multiple of 16 bytes,
+// so 4 columns for FP32 and FP64 alike) and kH rows above and below.
+constexpr int kTX = 32, kH = 3, kTL = 4, kWarps = 8;
 
 template <typename T>
 __device__ __forceinline__ T pick(float f, double d);
@@ -170,7 +177,7 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
 template <int TY>
 constexpr int tile_sw()
 {
-    return kTX + 2 * kH;
+    return kTX + 8;  // columns i0-4 .. i0+35
 }
 template <int TY>
 constexpr int tile_sh()
@@ -198,36 +205,19 @@ __device__ __forceinline__ void cp_async_elem(T *dst, const T *src, bool ok)
                      : "memory");
 }
 
-// Copies of the halo tile of `item` (4 planes, SH x SW) into sq, issued by
-// the whole block and committed as one group; points outside the instance
-// are zero.
+// The halo tile of `item` (4 planes, SH x SW, from (i0-4, j0-3)) into sqbuf
+// by one TMA load, counted by bar; points outside the instance read as zero.
+// Issued by thread 0.
 template <typename T, int TY>
-__device__ void tile_issue(const Args &a, int4 item, const T *qin, T *sqbuf)
+__device__ void tile_issue(const Args &a, int4 item, int which, T *sqbuf,
+                           unsigned long long *bar)
 {
     constexpr int SW = tile_sw<TY>(), SH = tile_sh<TY>();
-    T(*sq)[SH][SW] = reinterpret_cast<T(*)[SH][SW]>(sqbuf);
-    NS_CHECK(a.err, kChkBatch, item.x >= 0 && item.x < a.ninst);
-    const Inst in = a.inst[item.x];
-    const int i0 = item.y, j0 = item.z;
-    // a tile of kTX x TY points inside its instance; 8 warps of 32 lanes
-    NS_CHECK(a.err, kChkBatch, blockDim.x == 32 * kWarps && i0 >= 0 && i0 % kTX == 0 &&
-                                   i0 < in.imax && j0 >= 0 && j0 % TY == 0 && j0 < in.jmax &&
-                                   in.pitch >= in.imax);
-    const long long plane = (long long)in.pitch * in.jmax;
-    const T *q = qin + in.q_off;
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    for (int r = ty; r < SH; r += kWarps) {
-        const int gj = j0 - kH + r;
-        const bool rowok = gj >= 0 && gj < in.jmax;
-        for (int cc = tx; cc < SW; cc += kTX) {
-            const int gi = i0 - kH + cc;
-            const bool ok = rowok && gi >= 0 && gi < in.imax;
-            const long long g = ok ? (long long)gj * in.pitch + gi : 0;
-#pragma unroll
-            for (int k = 0; k < 4; k++) cp_async_elem(&sq[k][r][cc], q + k * plane + g, ok);
-        }
-    }
-    asm volatile("cp.async.commit_group;" ::: "memory");
+    NS_CHECK(a.err, kChkBatch, item.x >= 0 && item.x < a.ninst && item.y % kTX == 0 &&
+                                   ((item.y - kTL) * (int)sizeof(T)) % 16 == 0);
+    const CUtensorMap *map = a.qmaps + ((size_t)(TY == 16) * a.ninst + item.x) * 2 + which;
+    mbar_expect_tx(bar, (unsigned)(4 * SH * SW * sizeof(T)));
+    tma_load_3d(sqbuf, map, item.y - kTL, item.z - kH, 0, bar);
 }
 
 template <int N>
@@ -246,7 +236,7 @@ __device__ void stage_tile(const Args &a, int st, int4 item, const T *qin, T *qo
     NS_CHECK(a.err, kChkBatch, item.x >= 0 && item.x < a.ninst);
     const Inst in = a.inst[item.x];
     const int i0 = item.y, j0 = item.z;
-    // tile rows ly + kH +- 3 < SH and columns tx + kH +- 3 < SW; closures
+    // tile rows ly + kH +- 3 < SH and columns tx + kTL +- 3 < SW; closures
     // need lines of at least 7 points
     NS_CHECK(a.err, kChkBatch, blockDim.x == 32 * kWarps && TY % kWarps == 0 && i0 >= 0 &&
                                    i0 < in.imax && j0 >= 0 && j0 < in.jmax && in.imax >= 7 &&
@@ -267,7 +257,7 @@ __device__ void stage_tile(const Args &a, int st, int4 item, const T *qin, T *qo
             const int j = j0 + ly;
             if (j >= in.jmax) break;
             const long long idx = (long long)j * in.pitch + i;
-            const int sr = ly + kH, sc = tx + kH;
+            const int sr = ly + kH, sc = tx + kTL;
             const T *cyp = tab<T>(a.yc) + (long long)kCoefStride * (in.y_off + j);
             const float *cyl = a.ycl + (long long)kCoefStride * (in.y_off + j);
             const bool yint = (j >= 3 && j < in.jmax - 3);
@@ -363,7 +353,7 @@ __device__ void stage_tile(const Args &a, int st, int4 item, const T *qin, T *qo
                 for (int k = 0; k < 4; k++) {
                     const double dr = to_d<T>(pick<T>(in.dt_f, in.dt_d) * r[k]);
                     const double w = (st == 0) ? dr : fma(a.alpha[st], Wp[k * plane], dr);
-                    Wp[k * plane] = w;
+                    if (st < 5) Wp[k * plane] = w;  // stage 0 sets w = dt*R
                     qv[k] = from_d<T>(fma(a.beta[st], w, to_d<T>(qv[k])));
                 }
             }
@@ -592,13 +582,7 @@ __device__ void fx_item(const Args &a, int4 item, const T *srcq, T *dstq,
             for (int u = 6; u < 12; u++) w[u] = w[u + 1];
             w[12] = nxt;
         };
-        if (nstep == PW) {
-            // a whole block unrolled: the window slides by register renaming
-#pragma unroll
-            for (int t = 0; t < PW; t++) step(t);
-        } else {
-            for (int t = 0; t < nstep; t++) step(t);
-        }
+        for (int t = 0; t < nstep; t++) step(t);
         __syncwarp();
         for (int r = 0; r < nrows; r++)
             for (int x = lane; x < PW; x += 32) {
@@ -615,11 +599,16 @@ __device__ void fx_item(const Args &a, int4 item, const T *srcq, T *dstq,
     }
 }
 
-// Phase D: ccpml of one instance, one warp.
+// Phase D: ccpml of one instance at positions item.y .. item.y+31 (rows of
+// the left and right columns, columns of the top and bottom rows), one warp.
+// Every position's values are independent of the others' (the corner
+// columns recompute the column values they extrapolate from), so the
+// perimeter splits into pieces freely.
 template <typename T>
-__device__ void bc_item(const Args &a, int inst, T *qall)
+__device__ void bc_item(const Args &a, int2 item, T *qall)
 {
-    NS_CHECK(a.err, kChkBatch, inst >= 0 && inst < a.ninst);
+    const int inst = item.x;
+    NS_CHECK(a.err, kChkBatch, inst >= 0 && inst < a.ninst && item.y >= 0 && item.y % 32 == 0);
     const Inst in = a.inst[inst];
     const long long P = (long long)in.pitch * in.jmax;
     T *q = qall + in.q_off;
@@ -638,7 +627,9 @@ __device__ void bc_item(const Args &a, int inst, T *qall)
         }
     };
     const int nt = max(in.imax, in.jmax);
-    for (int t = threadIdx.x & 31; t < nt; t += 32) {
+    {
+        const int t = item.y + (threadIdx.x & 31);
+        if (t >= nt) return;
         T v[4];
         if (t > 0 && t < in.jmax - 1) {
             const long long r = (long long)t * in.pitch;
@@ -703,34 +694,47 @@ __device__ __forceinline__ void stamp(const Args &a, int slot)
 template <typename T, int TY>
 __global__ void __launch_bounds__(256) k_batch_step(Args a)
 {
-    extern __shared__ __align__(16) unsigned char smem[];
+    extern __shared__ __align__(128) unsigned char smem[];
     constexpr int PW = sizeof(T) == 4 ? 32 : 16;
     const int warp = threadIdx.x >> 5;
     // this warp's two x-line tiles of 32 rows
     T(*tx2)[32][PW + 1] = reinterpret_cast<T(*)[32][PW + 1]>(smem) + (size_t)warp * 2;
     const long long nwarps = (long long)gridDim.x * kWarps;
     const long long gw = (long long)blockIdx.x * kWarps + warp;
+    // one mbarrier per tile buffer; tuse counts the completed phases of
+    // both, buffer 0 in the low half and buffer 1 in the high half
+    __shared__ alignas(8) unsigned long long tbar[2];
+    unsigned tuse = 0u;
+    if (threadIdx.x == 0) {
+        mbar_init(&tbar[0], 1);
+        mbar_init(&tbar[1], 1);
+    }
+    __syncthreads();
     stamp(a, 0);
     for (int st = 0; st < 6; st++) {
         T *qa = reinterpret_cast<T *>((st & 1) ? a.q1 : a.q0);
         T *qb = reinterpret_cast<T *>((st & 1) ? a.q0 : a.q1);
         {
-            // two tile buffers: the next item's copies are in flight while
-            // the current item is computed
+            // two tile buffers: the next item's TMA load is in flight while
+            // the current item is computed.  The region was last written and
+            // read by the generic proxy (the previous phases): fence before
+            // the async proxy writes it.
             constexpr size_t kTile = 4 * (size_t)tile_sh<TY>() * tile_sw<TY>();
-            T *buf[2] = {reinterpret_cast<T *>(smem), reinterpret_cast<T *>(smem) + kTile};
+            T *const buf0 = reinterpret_cast<T *>(smem);
+            auto buf = [&](int x) { return buf0 + x * kTile; };
+            const int which = st & 1;  // qa is q1 in odd stages
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncthreads();
             int b = 0;
-            if ((int)blockIdx.x < a.ntiles) tile_issue<T, TY>(a, a.tiles[blockIdx.x], qa, buf[0]);
+            if (threadIdx.x == 0 && (int)blockIdx.x < a.ntiles)
+                tile_issue<T, TY>(a, a.tiles[blockIdx.x], which, buf(0), &tbar[0]);
             for (int it = blockIdx.x; it < a.ntiles; it += gridDim.x) {
                 const int nx = it + (int)gridDim.x;
-                if (nx < a.ntiles) {
-                    tile_issue<T, TY>(a, a.tiles[nx], qa, buf[b ^ 1]);
-                    tile_wait<1>();
-                } else {
-                    tile_wait<0>();
-                }
-                __syncthreads();
-                stage_tile<T, TY>(a, st, a.tiles[it], qa, qb, buf[b]);
+                if (threadIdx.x == 0 && nx < a.ntiles)
+                    tile_issue<T, TY>(a, a.tiles[nx], which, buf(b ^ 1), &tbar[b ^ 1]);
+                if (!mbar_wait_bounded(&tbar[b], (tuse >> (16 * b)) & 1u, a.err)) return;
+                tuse += 1u << (16 * b);
+                stage_tile<T, TY>(a, st, a.tiles[it], qa, qb, buf(b));
                 __syncthreads();  // buf[b] is refilled two items on
                 b ^= 1;
             }
@@ -817,7 +821,8 @@ struct ns_batch {
     ns::batch::Inst *inst = nullptr;
     int4 *tiles[2] = {nullptr, nullptr}, *fx = nullptr, *fy = nullptr;
     int ntiles[2] = {0, 0}, nfx = 0, nfy = 0, nbc = 0;
-    int *bc = nullptr;
+    int2 *bc = nullptr;
+    CUtensorMap *qmaps = nullptr;  // [(ty16 * n + inst) * 2 + buf]
     void *xc = nullptr, *yc = nullptr, *sigx = nullptr, *sigy = nullptr, *rho_bc = nullptr,
          *mrho = nullptr, *mu = nullptr, *mdrho = nullptr, *mdu = nullptr, *corr = nullptr;
     float *xcl = nullptr, *ycl = nullptr;
@@ -907,7 +912,7 @@ void bfree(ns_batch *b)
     void *ps[] = {b->q[0], b->q[1], b->W, b->stage_sin, b->wf, b->dtv, b->drho, b->du,
                   b->stagebuf, b->inst, b->tiles[0], b->tiles[1], b->fx, b->fy, b->bc,
                   b->xc, b->xcl, b->yc, b->ycl, b->sigx, b->sigy, b->rho_bc, b->mrho, b->mu,
-                  b->mdrho, b->mdu, b->corr, b->src, b->bar, b->err, b->d_iter};
+                  b->mdrho, b->mdu, b->corr, b->src, b->bar, b->err, b->d_iter, b->qmaps};
     for (void *p : ps)
         if (p) cudaFree(p);
     if (b->own) cudaStreamDestroy(b->own);
@@ -957,7 +962,7 @@ size_t smem_for(int precision, int ty)
 {
     const size_t es = precision == NS_PREC_SPLIT32 ? 4 : 8;
     const int pw = precision == NS_PREC_SPLIT32 ? 32 : 16;
-    const size_t tile = 2 * 4 * (size_t)(ty + 6) * 38 * es;  // two tile buffers
+    const size_t tile = 2 * 4 * (size_t)(ty + 6) * 40 * es;  // two tile buffers
     const size_t fx = (size_t)ns::batch::kWarps * 2 * 32 * (pw + 1) * es;
     return std::max(tile, fx);
 }
@@ -1188,7 +1193,7 @@ int ns_batch_create(const ns_params *const *params, int n, int precision, ns_bat
     b->stream = b->own;
     // work lists
     std::vector<int4> tiles8, tiles16, fxl, fyl;
-    std::vector<int> bcl;
+    std::vector<int2> bcl;
     for (int q = 0; q < n; q++) {
         const auto &in = hin[q];
         for (int j0 = 0; j0 < in.jmax; j0 += 8)
@@ -1201,7 +1206,8 @@ int ns_batch_create(const ns_params *const *params, int n, int precision, ns_bat
             for (int c0 = 0; c0 < in.imax; c0 += 32)
                 for (int c = 0; c < in.fy_chunks; c++) fyl.push_back(make_int4(q, k, c0, c));
         }
-        bcl.push_back(q);
+        // the perimeter in pieces of 32 positions, one warp each
+        for (int t0 = 0; t0 < std::max(in.imax, in.jmax); t0 += 32) bcl.push_back(make_int2(q, t0));
     }
     // filter items largest first: a chunk after the first also runs the warm-up
     auto item_cost = [&](const int4 &it, bool along_x) {
@@ -1260,6 +1266,44 @@ int ns_batch_create(const ns_params *const *params, int n, int precision, ns_bat
     B_TRY(balloc(b, &b->bar, 2 + 12));
     B_TRY(balloc(b, &b->err, 1));
     B_TRY(balloc(b, &b->d_iter, 1));
+    {
+        // the halo-tile maps of every instance, buffer and tile height: planes
+        // of jmax rows of pitch elements from the instance's plane 0; box
+        // 40 x (TY + 6) x 4 from (i0-4, j0-3), zeros outside the instance
+        const auto encode = ns::tensor_encoder();
+        if (!encode) {
+            rc = berr(b, NS_ERR_UNSUPPORTED, "ns_batch_create: cuTensorMapEncodeTiled is unavailable");
+            goto fail;
+        }
+        std::vector<CUtensorMap> maps((size_t)4 * n);
+        for (int t16 = 0; t16 < 2; t16++)
+            for (int q = 0; q < n; q++)
+                for (int bf = 0; bf < 2; bf++) {
+                    const auto &in = hin[q];
+                    const cuuint64_t dims[3] = {(cuuint64_t)in.imax, (cuuint64_t)in.jmax, 4};
+                    const cuuint64_t strides[2] = {(cuuint64_t)in.pitch * es,
+                                                   (cuuint64_t)in.pitch * in.jmax * es};
+                    const cuuint32_t box[3] = {(cuuint32_t)(ns::batch::kTX + 8),
+                                               (cuuint32_t)((t16 ? 16 : 8) + 2 * ns::batch::kH), 4};
+                    const cuuint32_t estr[3] = {1u, 1u, 1u};
+                    void *base = (unsigned char *)b->q[bf] + (size_t)in.q_off * es;
+                    const CUresult r = encode(
+                        &maps[((size_t)t16 * n + q) * 2 + bf],
+                        es == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64,
+                        3, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                        CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                    if (r != CUDA_SUCCESS) {
+                        rc = berr(b, NS_ERR_CUDA, "ns_batch_create: cuTensorMapEncodeTiled failed");
+                        goto fail;
+                    }
+                }
+        rc = balloc(b, &b->qmaps, maps.size());
+        if (rc == NS_OK) rc = bput(b, b->qmaps, maps);
+        if (rc == NS_OK && cudaStreamSynchronize(b->stream) != cudaSuccess)
+            rc = berr(b, NS_ERR_CUDA, "ns_batch_create: tensor map upload");
+        if (rc != NS_OK) goto fail;
+    }
     if (cudaMemsetAsync(b->q[0], 0, b->qsize * es, b->stream) != cudaSuccess ||
         cudaMemsetAsync(b->q[1], 0, b->qsize * es, b->stream) != cudaSuccess ||
         cudaMemsetAsync(b->W, 0, b->wsize * 8, b->stream) != cudaSuccess ||
@@ -1327,6 +1371,7 @@ int ns_batch_create(const ns_params *const *params, int n, int precision, ns_bat
         a.nfy = b->nfy;
         a.nbc = b->nbc;
         a.ninst = b->n;
+        a.qmaps = b->qmaps;
         a.q0 = b->q[0];
         a.q1 = b->q[1];
         a.W = b->W;
@@ -1636,7 +1681,7 @@ int ns_batch_info(ns_batch *b, int *grid, int *ty, int *blocks_per_sm, int *item
         items[0] = b->ntiles[b->ty == 8 ? 0 : 1];
         items[1] = b->nfx;
         items[2] = b->nfy;
-        items[3] = b->nbc;
+        items[3] = b->n;
     }
     return NS_OK;
 }

@@ -8,6 +8,7 @@
 #pragma once
 
 #include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string>
@@ -132,6 +133,17 @@ struct SplitMean {
     float p, gamma;
 };
 
+// Constants of the split-precision viscous terms (Navier-Stokes with a
+// base flow uniform in x and y, v = 0): T' = T - T_b from rho' and p',
+// mu(T) and k(T) from the FP32 copy of the transport table (or, outside it,
+// the fit by expf/logf with x = Tref*T), and the factors of
+// eqeuler.f90:68-92.
+struct SplitVisc {
+    float rho_b, p_b, gamma, T_b;     // uniform base flow, T_b = gamma*p_b/rho_b
+    float inv_re, gm1_re, inv_re_pr;  // 1/Re, (gamma-1)/Re, 1/(Re*Pr)
+    float Tref, A_mi, B_mi, C_mi, D_mi_s, A_k, B_k, C_k, D_k_s;
+};
+
 // Device state of the split-precision path (precision = NS_PREC_SPLIT).
 struct SplitState {
     int fpitch = 0;                   // FP32 row pitch (elements)
@@ -150,6 +162,13 @@ struct SplitState {
     SplitMean mean{};
     double p_bc = 0.0;                // 1/gamma - p_b
     int warm = 0, fx_chunks = 1, fy_chunks = 1;
+    // viscous (Navier-Stokes) only: tau_xx', tau_xy', tau_yy', k dT'/dx,
+    // k dT'/dy as FP32 planes, their TMA map (imax, jmax, 5), the transport
+    // table rounded to FP32 and the constants
+    float *tau = nullptr;
+    CUtensorMap vmap;
+    float *trf = nullptr;
+    SplitVisc vis{};
 };
 
 }  // namespace ns
@@ -253,6 +272,9 @@ cudaError_t launch_rows_to_planes(const double *rows, double *planes, const Dims
 int count_step_launches(const ns_ctx *c);
 // Makes msg the text ns_last_error(NULL) returns (ns_api.cu).
 void record_error(const char *msg);
+// cuTensorMapEncodeTiled through the runtime's driver entry point, or null
+// when it is unavailable (ns_api.cu).
+PFN_cuTensorMapEncodeTiled_v12000 tensor_encoder();
 // NS_ERR_CHECK for an error word a failed index check of the checked build
 // left (ns_check.cuh), with the file and line as the error text (ns_api.cu).
 int check_error(int word);

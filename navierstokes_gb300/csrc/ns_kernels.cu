@@ -609,11 +609,11 @@ void filter_shape(int nlines, int n, int nk, int warm, int nsm, int kw, long lon
 }
 
 // ---------------------------------------------------------------------------
-// k_bc: ccpml (cc.f90:6-68).  Thread t < jmax sets row t of the left and
-// right columns (cc.f90:23-36, corners excepted); thread t < imax sets
-// column t of the top and bottom rows (cc.f90:39-59), recomputing the
-// column values it extrapolates from at i = 1 and i = imax, so no thread
-// reads a location another thread writes.
+// k_bc: ccpml (cc.f90:6-68).  Row t of the left and right columns
+// (cc.f90:23-36, corners excepted) and column t of the top and bottom rows
+// (cc.f90:39-59); the corner columns recompute the column values they
+// extrapolate from at i = 1 and i = imax, so no thread reads a location
+// another thread writes.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void bc_column_values(const double *__restrict__ U, const Dims &d,
                                                  int i, int j, const double *__restrict__ rhob,
@@ -635,49 +635,44 @@ __device__ __forceinline__ void bc_column_values(const double *__restrict__ U, c
     }
 }
 
+// blockIdx.y picks the edge: 0 left, 1 right (rows t), 2 top, 3 bottom
+// (columns t).  The four write disjoint locations and read only points no
+// edge writes, so they run side by side, one memory round trip each.
 __global__ void k_bc(Dims d, double *__restrict__ U, const double *__restrict__ rhob,
                      const double *__restrict__ psib, double gamma)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int edge = blockIdx.y;
     const long long P = d.plane;
     double v[kMaxNk];
-    if (t > 0 && t < d.jmax - 1) {
-        const long long r = (long long)t * d.pitch;
-        bc_column_values(U, d, 0, t, rhob, psib, gamma, v);
-        for (int k = 0; k < d.nk; k++) U[k * P + r] = v[k];
-        bc_column_values(U, d, d.imax - 1, t, rhob, psib, gamma, v);
-        for (int k = 0; k < d.nk; k++) U[k * P + r + d.imax - 1] = v[k];
-    }
-    if (t < d.imax) {
-        const int jt = d.jmax - 1;
-        double a[kMaxNk], b[kMaxNk];
-        // top (cc.f90:39-43)
-        if (t == 0 || t == d.imax - 1) {
-            bc_column_values(U, d, t, jt - 1, rhob, psib, gamma, a);
-            bc_column_values(U, d, t, jt - 2, rhob, psib, gamma, b);
-        } else {
-            for (int k = 0; k < d.nk; k++) {
-                a[k] = U[k * P + (long long)(jt - 1) * d.pitch + t];
-                b[k] = U[k * P + (long long)(jt - 2) * d.pitch + t];
-            }
+    if (edge < 2) {
+        if (t > 0 && t < d.jmax - 1) {
+            const long long r = (long long)t * d.pitch;
+            const int i = edge == 0 ? 0 : d.imax - 1;
+            bc_column_values(U, d, i, t, rhob, psib, gamma, v);
+            for (int k = 0; k < d.nk; k++) U[k * P + r + i] = v[k];
         }
-        for (int k = 0; k < 3; k++) U[k * P + (long long)jt * d.pitch + t] = 2.0 * a[k] - b[k];
-        U[3 * P + (long long)jt * d.pitch + t] = 1.0 / gamma;
-        if (d.nk >= 5) U[4 * P + (long long)jt * d.pitch + t] = 1.0;
-        // bottom (cc.f90:55-59)
-        if (t == 0 || t == d.imax - 1) {
-            bc_column_values(U, d, t, 1, rhob, psib, gamma, a);
-            bc_column_values(U, d, t, 2, rhob, psib, gamma, b);
-        } else {
-            for (int k = 0; k < d.nk; k++) {
-                a[k] = U[k * P + (long long)1 * d.pitch + t];
-                b[k] = U[k * P + (long long)2 * d.pitch + t];
-            }
-        }
-        for (int k = 0; k < 3; k++) U[k * P + t] = 2.0 * a[k] - b[k];
-        U[3 * P + t] = 1.0 / gamma;
-        if (d.nk >= 5) U[4 * P + t] = 0.0;
+        return;
     }
+    if (t >= d.imax) return;
+    const bool top = edge == 2;
+    // top (cc.f90:39-43) from rows jt-1, jt-2; bottom (cc.f90:55-59) from rows 1, 2
+    const int jt = d.jmax - 1;
+    const int j1 = top ? jt - 1 : 1, j2 = top ? jt - 2 : 2, jw = top ? jt : 0;
+    double a[kMaxNk], b[kMaxNk];
+    if (t == 0 || t == d.imax - 1) {
+        bc_column_values(U, d, t, j1, rhob, psib, gamma, a);
+        bc_column_values(U, d, t, j2, rhob, psib, gamma, b);
+    } else {
+        for (int k = 0; k < d.nk; k++) {
+            a[k] = U[k * P + (long long)j1 * d.pitch + t];
+            b[k] = U[k * P + (long long)j2 * d.pitch + t];
+        }
+    }
+    const long long w = (long long)jw * d.pitch + t;
+    for (int k = 0; k < 3; k++) U[k * P + w] = 2.0 * a[k] - b[k];
+    U[3 * P + w] = 1.0 / gamma;
+    if (d.nk >= 5) U[4 * P + w] = top ? 1.0 : 0.0;
 }
 
 // ---------------------------------------------------------------------------
@@ -845,7 +840,7 @@ static cudaError_t launch_kernel_t(ns_ctx *c, int cls, int stage, cudaStream_t s
     }
     case NS_KC_BC: {
         const int nt = d.imax > d.jmax ? d.imax : d.jmax;
-        k_bc<<<(nt + 127) / 128, 128, 0, s>>>(d, c->U, c->rhob, c->psib, c->phys.gamma);
+        k_bc<<<dim3((nt + 127) / 128, 4), 128, 0, s>>>(d, c->U, c->rhob, c->psib, c->phys.gamma);
         break;
     }
     case NS_KC_STAGE_SIN: {
@@ -880,6 +875,7 @@ int step_sequence(const ns_ctx *c, int *cls, int *stage)
     if (c->src || c->sp.src) { cls[n] = NS_KC_STAGE_SIN; stage[n++] = 0; }
     if (c->split) {
         for (int st = 0; st < 6; st++) {
+            if (c->visc) { cls[n] = NS_KC_SPLIT_VISC; stage[n++] = st; }
             cls[n] = NS_KC_SPLIT_STAGE; stage[n++] = st;
             cls[n] = NS_KC_SPLIT_FX; stage[n++] = st;
             cls[n] = NS_KC_SPLIT_FY; stage[n++] = st;

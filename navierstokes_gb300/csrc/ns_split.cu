@@ -178,9 +178,158 @@ __device__ __forceinline__ void pair_scale(float &h, float &l, float s)
     h = p;
 }
 
-template <int NP, bool FIRST, bool SRC>
+// ---------------------------------------------------------------------------
+// Viscous terms (Navier-Stokes, base flow uniform in x and y with v = 0):
+// the base flow's own stresses and heat flux vanish, so tau and k grad T
+// are perturbation-sized and FP32 carries them.
+// ---------------------------------------------------------------------------
+// T' = T - T_b for T = gamma*p/rho (rhs.f90:20) written without the
+// cancellation of two O(1) temperatures:
+// T' = gamma*(p'*rho_b - p_b*rho') / (rho_b*(rho_b + rho')).
+__device__ __forceinline__ float t_prime(float rho1, float p1, const SplitVisc &v)
+{
+    const float num = fmaf(p1, v.rho_b, -(v.p_b * rho1));
+    return v.gamma * num / (v.rho_b * (v.rho_b + rho1));
+}
+
+// mu(T) and k(T) with 1/mu0, 1/k0 folded in (coefficients.f90:27-59): the
+// FP32 copy of the context's piecewise-polynomial table (the piece from the
+// exponent and the top 8 fraction bits of T, Horner in u = T minus the
+// piece's left end, exact by Sterbenz), else the fit itself by logf/expf.
+__device__ __forceinline__ void transport_f32(float T, const float *__restrict__ trf,
+                                              const SplitVisc &v, float &mu, float &kc)
+{
+    const unsigned b = __float_as_uint(T);
+    const int e = (int)((b >> 23) & 0xffu) - 127;
+    if (!(b >> 31) && e >= kTrEmin && e < kTrEmin + kTrOctaves) {
+        const int piece = ((e - kTrEmin) << 8) | (int)((b >> 15) & 255u);
+        const float u = T - __uint_as_float(b & 0xffff8000u);
+        const float *c = trf + (size_t)piece * kTrStride;
+        mu = fmaf(fmaf(fmaf(fmaf(fmaf(c[5], u, c[4]), u, c[3]), u, c[2]), u, c[1]), u, c[0]);
+        kc = fmaf(fmaf(fmaf(fmaf(fmaf(c[11], u, c[10]), u, c[9]), u, c[8]), u, c[7]), u, c[6]);
+        return;
+    }
+    const float x = v.Tref * T;
+    const float L = logf(x), y = 1.0f / x;
+    mu = expf(fmaf(v.A_mi, L, fmaf(fmaf(v.C_mi, y, v.B_mi), y, v.D_mi_s)));
+    kc = expf(fmaf(v.A_k, L, fmaf(fmaf(v.C_k, y, v.B_k), y, v.D_k_s)));
+}
+
+// T' at point (i, j) from global memory (closure points near the edges).
+template <int NP>
+__device__ __forceinline__ float t_prime_at(const float *__restrict__ q, long long fplane,
+                                            long long idx, const SplitVisc &v)
+{
+    float p1 = q[3 * fplane + idx];
+    if (NP >= 3) p1 += q[6 * fplane + idx];
+    return t_prime(q[idx], p1, v);
+}
+
+// tau' (eqeuler.f90:37-39) and k grad T' (derivs.f90:48-56) of the
+// perturbation, at every point: five FP32 planes for the stage kernel.  The
+// halo tile of q' arrives by TMA as in the stage kernel; T' is formed for
+// every tile point in shared memory, then differentiated there (closures:
+// from global memory).  Velocity gradients use the hi parts: their lo parts
+// are below 2^-24 of them and the stresses enter the right-hand side times
+// 1/Re.
+template <int NP>
 __global__ void __launch_bounds__(256, kSplitMinBlocks)
-    k_split_stage(const __grid_constant__ CUtensorMap qmap, int *__restrict__ err, Dims d,
+    k_split_visc(const __grid_constant__ CUtensorMap qmap, int *__restrict__ err, Dims d,
+                 int fpitch, const float *__restrict__ q, float *__restrict__ tau,
+                 const float *__restrict__ xc, const float *__restrict__ yc,
+                 const float *__restrict__ trf, const SplitVisc v)
+{
+    constexpr int kTX_ = 32, kTY_ = kSplitTY, kH_ = 3, kSH_ = kTY_ + 2 * kH_;
+    constexpr int kTL_ = 4, kSW_ = 40, NPL = 4 + NP;
+    __shared__ alignas(128) float sq[NPL][kSH_][kSW_];
+    __shared__ float sT[kSH_][kSW_];
+    __shared__ alignas(8) unsigned long long tbar;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int i0 = blockIdx.x * kTX_, j0 = blockIdx.y * kTY_;
+    const long long fplane = (long long)fpitch * d.jmax;
+    const bool lead = (tx == 0 && ty == 0);
+    NS_CHECK(err, kChkSplit, blockDim.x == kTX_ && blockDim.y == 8 && kTY_ % 8 == 0);
+    NS_CHECK(err, kChkSplit, ((i0 - kTL_) & 3) == 0 && fpitch >= d.imax && d.imax >= 7 &&
+                                 d.jmax >= 7);
+    if (lead) mbar_init(&tbar, 1);
+    __syncthreads();
+    if (lead) {
+        mbar_expect_tx(&tbar, (unsigned)sizeof(sq));
+        tma_load_3d(&sq[0][0][0], &qmap, i0 - kTL_, j0 - kH_, 0, &tbar);
+    }
+    if (!mbar_wait_bounded(&tbar, 0, err)) return;
+    const int tid = ty * kTX_ + tx;
+    for (int e = tid; e < kSH_ * kSW_; e += kTX_ * 8) {
+        const int r = e / kSW_, c = e % kSW_;
+        float p1 = sq[3][r][c];
+        if (NP >= 3) p1 += sq[6][r][c];
+        sT[r][c] = t_prime(sq[0][r][c], p1, v);
+    }
+    __syncthreads();
+    const int i = i0 + tx;
+    if (i >= d.imax) return;
+    const float *cxp = xc + kCoefStride * i;
+    const bool xint = (i >= 3 && i < d.imax - 3);
+#pragma unroll
+    for (int h = 0; h < kTY_ / 8; h++) {
+        const int ly = ty + 8 * h;
+        const int j = j0 + ly;
+        if (j >= d.jmax) break;
+        const long long fidx = (long long)j * fpitch + i;
+        const int sr = ly + kH_, sc = tx + kTL_;
+        const float *cyp = yc + kCoefStride * j;
+        const bool yint = (j >= 3 && j < d.jmax - 3);
+        // x and y derivatives of a tile plane, closures from global memory
+        auto ddx = [&](const float (*t)[kSW_], auto glob) -> float {
+            if (xint) {
+                float r = cxp[4] * (t[sr][sc + 1] - t[sr][sc - 1]);
+                r = fmaf(cxp[5], t[sr][sc + 2] - t[sr][sc - 2], r);
+                return fmaf(cxp[6], t[sr][sc + 3] - t[sr][sc - 3], r);
+            }
+            const int o0 = (i < 3) ? -i : (d.imax - 7 - i);
+            const float f0 = glob(fidx);
+            float r = 0.f;
+#pragma unroll
+            for (int z = 0; z < 7; z++) r = fmaf(cxp[z], glob(fidx + o0 + z) - f0, r);
+            return r;
+        };
+        auto ddy = [&](const float (*t)[kSW_], auto glob) -> float {
+            if (yint) {
+                float r = cyp[4] * (t[sr + 1][sc] - t[sr - 1][sc]);
+                r = fmaf(cyp[5], t[sr + 2][sc] - t[sr - 2][sc], r);
+                return fmaf(cyp[6], t[sr + 3][sc] - t[sr - 3][sc], r);
+            }
+            const int o0 = (j < 3) ? -j : (d.jmax - 7 - j);
+            const float f0 = glob(fidx);
+            float r = 0.f;
+#pragma unroll
+            for (int z = 0; z < 7; z++)
+                r = fmaf(cyp[z], glob(fidx + (long long)(o0 + z) * fpitch) - f0, r);
+            return r;
+        };
+        auto gu = [&](long long x) { return q[fplane + x]; };
+        auto gv = [&](long long x) { return q[2 * fplane + x]; };
+        auto gT = [&](long long x) { return t_prime_at<NP>(q, fplane, x, v); };
+        const float ux = ddx(sq[1], gu), uy = ddy(sq[1], gu);
+        const float vx = ddx(sq[2], gv), vy = ddy(sq[2], gv);
+        const float Tx = ddx(sT, gT), Ty = ddy(sT, gT);
+        float mu, kc;
+        transport_f32(v.T_b + sT[sr][sc], trf, v, mu, kc);
+        const float div = ux + vy;
+        const float m23 = (2.0f / 3.0f) * mu, mu2 = 2.0f * mu;
+        tau[fidx] = fmaf(mu2, ux, -(m23 * div));
+        tau[fplane + fidx] = mu * (uy + vx);
+        tau[2 * fplane + fidx] = fmaf(mu2, vy, -(m23 * div));
+        tau[3 * fplane + fidx] = kc * Tx;
+        tau[4 * fplane + fidx] = kc * Ty;
+    }
+}
+
+template <int NP, bool FIRST, bool SRC, bool VISC>
+__global__ void __launch_bounds__(256, VISC ? 3 : kSplitMinBlocks)
+    k_split_stage(const __grid_constant__ CUtensorMap qmap, const __grid_constant__ CUtensorMap vmap,
+                  const float *__restrict__ tau, const float *__restrict__ trf, const SplitVisc vis,
+                  int *__restrict__ err, Dims d,
                   int fpitch, const float *__restrict__ qin, float *__restrict__ qout,
                   double *__restrict__ W, const float *__restrict__ xc,
                   const float *__restrict__ yc, const float *__restrict__ xcl,
@@ -191,6 +340,8 @@ __global__ void __launch_bounds__(256, kSplitMinBlocks)
 {
     constexpr int NPL = 4 + NP;
     __shared__ alignas(128) float sq[NPL][kSH][kSW];
+    // viscous: the halo tile of tau_xx', tau_xy', tau_yy', k dT'/dx, k dT'/dy
+    __shared__ alignas(128) float sv[VISC ? 5 : 1][VISC ? kSH : 1][VISC ? kSW : 4];
     __shared__ alignas(8) unsigned long long tbar;
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int i0 = blockIdx.x * kTX, j0 = blockIdx.y * kTY;
@@ -206,8 +357,9 @@ __global__ void __launch_bounds__(256, kSplitMinBlocks)
     if (lead) {
         // the box (40 x kSH x NPL floats) starts at (i0-4, j0-3, 0); points
         // outside the grid read as zero and are never used
-        mbar_expect_tx(&tbar, (unsigned)sizeof(sq));
+        mbar_expect_tx(&tbar, (unsigned)(sizeof(sq) + (VISC ? sizeof(sv) : 0)));
         tma_load_3d(&sq[0][0][0], &qmap, i0 - kTL, j0 - kH, 0, &tbar);
+        if (VISC) tma_load_3d(&sv[0][0][0], &vmap, i0 - kTL, j0 - kH, 0, &tbar);
     }
     // the FP64 accumulators of this thread's two points, requested before
     // the tile so that their latency overlaps the tile load
@@ -333,12 +485,46 @@ __global__ void __launch_bounds__(256, kSplitMinBlocks)
             t = fmaf(gp, div, t);
             if (SRC) t = t - (float)stage_sin[stage] * src[fidx];
             r[3] = -t;
+            if (VISC) {
+                // eqeuler.f90:68-92: (1/(Re rho)) div tau for u and v,
+                // (gamma-1)/Re * Phi + 1/(Re Pr) * div(k grad T) for p
+                const long long vpl = fplane;
+                auto dxy = [&](int a, int b) -> float {
+                    float rx, ry;
+                    if (xint) {
+                        rx = cx4 * (sv[a][sr][sc + 1] - sv[a][sr][sc - 1]);
+                        rx = fmaf(cx5, sv[a][sr][sc + 2] - sv[a][sr][sc - 2], rx);
+                        rx = fmaf(cx6, sv[a][sr][sc + 3] - sv[a][sr][sc - 3], rx);
+                    } else {
+                        rx = closure_f32(tau + a * vpl + fidx, 1, i, d.imax, cxp);
+                    }
+                    if (yint) {
+                        ry = cyp[4] * (sv[b][sr + 1][sc] - sv[b][sr - 1][sc]);
+                        ry = fmaf(cyp[5], sv[b][sr + 2][sc] - sv[b][sr - 2][sc], ry);
+                        ry = fmaf(cyp[6], sv[b][sr + 3][sc] - sv[b][sr - 3][sc], ry);
+                    } else {
+                        ry = closure_f32(tau + b * vpl + fidx, fpitch, j, d.jmax, cyp);
+                    }
+                    return rx + ry;
+                };
+                const float rv = vis.inv_re * ri;
+                r[1] = fmaf(rv, dxy(0, 1), r[1]);
+                r[2] = fmaf(rv, dxy(1, 2), r[2]);
+                const float t0 = sv[0][sr][sc], t1 = sv[1][sr][sc], t2 = sv[2][sr][sc];
+                float phi = gx[1] * t0;
+                phi = fmaf(gx[2], t1, phi);
+                phi = fmaf(gy[1], t1, phi);
+                phi = fmaf(gy[2], t2, phi);
+                r[3] = fmaf(vis.gm1_re, phi, r[3]);
+                r[3] = fmaf(vis.inv_re_pr, dxy(3, 4), r[3]);
+            }
             // rk_steep (rk.f90:163-164): FP64 accumulator; u', v' kept as pairs
 #pragma unroll
             for (int k = 0; k < 4; k++) {
                 const double dr = f2d_exact(dt * r[k]);
                 const double w = FIRST ? dr : fma(alpha, wold[h][k], dr);
-                W[k * d.plane + didx] = w;
+                // stage 5's w is never read: stage 0 sets w = dt*R
+                if (stage < 5) W[k * d.plane + didx] = w;
                 if (is_pair<NP>(k)) {
                     // hi + beta*w in FP64, split exactly; the old lo joins in FP32
                     // (both parts are below an FP32 ulp of hi)
@@ -699,14 +885,7 @@ __device__ __forceinline__ void filter_x_rows(const float *__restrict__ sbase,
             wh[12] = nh;
             wl[12] = nl;
         };
-        if (nstep == 32) {
-            // a whole block unrolled: the window slides by register renaming
-            // instead of 26 moves per step, and the tile columns are constants
-#pragma unroll
-            for (int t = 0; t < 32; t++) step(t);
-        } else {
-            for (int t = 0; t < nstep; t++) step(t);
-        }
+        for (int t = 0; t < nstep; t++) step(t);
         __syncwarp();
         // write outputs q = qb .. qb+nstep-1 that this chunk owns (q >= a)
         for (int r = 0; r < nrows; r++) {
@@ -929,17 +1108,30 @@ static cudaError_t launch_split_np(ns_ctx *c, int cls, int stage, cudaStream_t s
     case NS_KC_SPLIT_STAGE: {
         const dim3 blk(kTX, 8), grd((d.imax + kTX - 1) / kTX, (d.jmax + kTY - 1) / kTY);
         const bool src = sp.src != nullptr;
-#define NS_SPL(FIRST, SRC)                                                                      \
-    k_split_stage<NP, FIRST, SRC><<<grd, blk, 0, s>>>(                                          \
-        sp.qmap[stage & 1], c->d_err, d, sp.fpitch, qa, qb, c->W, sp.xc, sp.yc, sp.xcl, sp.ycl,   \
-        sp.mean, sp.sigx, sp.sigy, sp.src, c->stage_sin, (float)c->p.dt, c->alpha[stage],        \
-        c->beta[stage], stage)
-        if (stage == 0) {
-            if (src) NS_SPL(true, true); else NS_SPL(true, false);
+#define NS_SPL(FIRST, SRC, VISC)                                                                \
+    k_split_stage<NP, FIRST, SRC, VISC><<<grd, blk, 0, s>>>(                                    \
+        sp.qmap[stage & 1], sp.vmap, sp.tau, sp.trf, sp.vis, c->d_err, d, sp.fpitch, qa, qb,    \
+        c->W, sp.xc, sp.yc, sp.xcl, sp.ycl, sp.mean, sp.sigx, sp.sigy, sp.src, c->stage_sin,    \
+        (float)c->p.dt, c->alpha[stage], c->beta[stage], stage)
+#define NS_SPL2(VISC)                                                                           \
+    if (stage == 0) {                                                                           \
+        if (src) NS_SPL(true, true, VISC); else NS_SPL(true, false, VISC);                      \
+    } else {                                                                                    \
+        if (src) NS_SPL(false, true, VISC); else NS_SPL(false, false, VISC);                    \
+    }
+        if (c->visc) {
+            NS_SPL2(true)
         } else {
-            if (src) NS_SPL(false, true); else NS_SPL(false, false);
+            NS_SPL2(false)
         }
+#undef NS_SPL2
 #undef NS_SPL
+        break;
+    }
+    case NS_KC_SPLIT_VISC: {
+        const dim3 blk(kTX, 8), grd((d.imax + kTX - 1) / kTX, (d.jmax + kTY - 1) / kTY);
+        k_split_visc<NP><<<grd, blk, 0, s>>>(sp.qmap[stage & 1], c->d_err, d, sp.fpitch, qa,
+                                             sp.tau, sp.xc, sp.yc, sp.trf, sp.vis);
         break;
     }
     case NS_KC_SPLIT_FX: {
