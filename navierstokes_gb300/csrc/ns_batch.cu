@@ -695,7 +695,12 @@ template <typename T, int TY>
 __global__ void __launch_bounds__(256) k_batch_step(Args a)
 {
     extern __shared__ __align__(128) unsigned char smem[];
-    constexpr int PW = sizeof(T) == 4 ? 32 : 16;
+    // x-line block width: 32 positions for FP32 with 16-row tiles, else 16.
+    // The FP32 8-row shape fits 64 registers, and with 16-position x-line
+    // tiles (35 KB instead of 68 KB per block) 4 blocks per SM instead of 3;
+    // the 16-row shape needs 80 registers and stays at 3 either way.  The
+    // autotuner picks between the two.
+    constexpr int PW = (sizeof(T) == 4 && TY == 16) ? 32 : 16;
     const int warp = threadIdx.x >> 5;
     // this warp's two x-line tiles of 32 rows
     T(*tx2)[32][PW + 1] = reinterpret_cast<T(*)[32][PW + 1]>(smem) + (size_t)warp * 2;
@@ -961,7 +966,7 @@ cudaError_t launch_step(ns_batch *b, cudaStream_t s, unsigned long long *stamps 
 size_t smem_for(int precision, int ty)
 {
     const size_t es = precision == NS_PREC_SPLIT32 ? 4 : 8;
-    const int pw = precision == NS_PREC_SPLIT32 ? 32 : 16;
+    const int pw = (precision == NS_PREC_SPLIT32 && ty == 16) ? 32 : 16;  // as k_batch_step
     const size_t tile = 2 * 4 * (size_t)(ty + 6) * 40 * es;  // two tile buffers
     const size_t fx = (size_t)ns::batch::kWarps * 2 * 32 * (pw + 1) * es;
     return std::max(tile, fx);
