@@ -691,16 +691,14 @@ __device__ __forceinline__ void stamp(const Args &a, int slot)
     }
 }
 
-template <typename T, int TY>
-__global__ void __launch_bounds__(256) k_batch_step(Args a)
+// TY: tile rows of phase A; PW: x-line block width of phase B (its two
+// tiles per warp set the shared memory, and with it how many blocks fit on
+// an SM).  The autotuner picks the shape.  The FP32 shapes fit 64 registers
+// without spilling, so 4 blocks per SM when the shared memory allows.
+template <typename T, int TY, int PW>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 1) k_batch_step(Args a)
 {
     extern __shared__ __align__(128) unsigned char smem[];
-    // x-line block width: 32 positions for FP32 with 16-row tiles, else 16.
-    // The FP32 8-row shape fits 64 registers, and with 16-position x-line
-    // tiles (35 KB instead of 68 KB per block) 4 blocks per SM instead of 3;
-    // the 16-row shape needs 80 registers and stays at 3 either way.  The
-    // autotuner picks between the two.
-    constexpr int PW = (sizeof(T) == 4 && TY == 16) ? 32 : 16;
     const int warp = threadIdx.x >> 5;
     // this warp's two x-line tiles of 32 rows
     T(*tx2)[32][PW + 1] = reinterpret_cast<T(*)[32][PW + 1]>(smem) + (size_t)warp * 2;
@@ -836,7 +834,7 @@ struct ns_batch {
     int *err = nullptr;
     int *d_iter = nullptr;
     ns::batch::Args args{};
-    int ty = 16, blocks_per_sm = 0, grid = 0;
+    int ty = 16, pw = 16, blocks_per_sm = 0, grid = 0;
     size_t smem = 0;
     double tuned_ms = 0.0;
     bool has_src = false, have_state = false;
@@ -923,15 +921,33 @@ void bfree(ns_batch *b)
     if (b->own) cudaStreamDestroy(b->own);
 }
 
-template <typename T, int TY>
-cudaError_t launch_step_t(ns_batch *b, cudaStream_t s, unsigned long long *stamps)
+using StepKernel = void (*)(ns::batch::Args);
+
+// The step kernel of a shape: precision, tile rows (8, 16) and x-line block
+// width (16, 24 or 32 positions for FP32, 16 for FP64).  For FP32 the
+// x-line tiles take 35, 51 or 68 KB per block: 4, 4 or 3 blocks fit on an
+// SM, and the more shared memory, the less L1 remains for the tile phase's
+// table and closure loads.  The autotuner measures which wins.
+StepKernel step_kernel(int precision, int ty, int pw)
+{
+    using ns::batch::k_batch_step;
+    if (precision == NS_PREC_SPLIT32) {
+        if (ty == 8)
+            return pw == 32 ? k_batch_step<float, 8, 32>
+                            : pw == 24 ? k_batch_step<float, 8, 24> : k_batch_step<float, 8, 16>;
+        return pw == 32 ? k_batch_step<float, 16, 32>
+                        : pw == 24 ? k_batch_step<float, 16, 24> : k_batch_step<float, 16, 16>;
+    }
+    return ty == 8 ? k_batch_step<double, 8, 16> : k_batch_step<double, 16, 16>;
+}
+
+cudaError_t launch_step_k(ns_batch *b, cudaStream_t s, unsigned long long *stamps)
 {
     ns::batch::Args a = b->args;
     a.stamps = stamps;
-    a.tiles = b->tiles[TY == 8 ? 0 : 1];
-    a.ntiles = b->ntiles[TY == 8 ? 0 : 1];
+    a.tiles = b->tiles[b->ty == 8 ? 0 : 1];
+    a.ntiles = b->ntiles[b->ty == 8 ? 0 : 1];
     a.nblocks = (unsigned)b->grid;
-    void *kargs[] = {&a};
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)b->grid);
     cfg.blockDim = dim3(256);
@@ -942,8 +958,7 @@ cudaError_t launch_step_t(ns_batch *b, cudaStream_t s, unsigned long long *stamp
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    (void)kargs;
-    return cudaLaunchKernelEx(&cfg, ns::batch::k_batch_step<T, TY>, a);
+    return cudaLaunchKernelEx(&cfg, step_kernel(b->precision, b->ty, b->pw), a);
 }
 
 cudaError_t launch_step(ns_batch *b, cudaStream_t s, unsigned long long *stamps = nullptr)
@@ -956,41 +971,33 @@ cudaError_t launch_step(ns_batch *b, cudaStream_t s, unsigned long long *stamps 
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
-    if (b->precision == NS_PREC_SPLIT32)
-        return b->ty == 8 ? launch_step_t<float, 8>(b, s, stamps)
-                          : launch_step_t<float, 16>(b, s, stamps);
-    return b->ty == 8 ? launch_step_t<double, 8>(b, s, stamps)
-                      : launch_step_t<double, 16>(b, s, stamps);
+    return launch_step_k(b, s, stamps);
 }
 
-size_t smem_for(int precision, int ty)
+size_t smem_for(int precision, int ty, int pw)
 {
     const size_t es = precision == NS_PREC_SPLIT32 ? 4 : 8;
-    const int pw = (precision == NS_PREC_SPLIT32 && ty == 16) ? 32 : 16;  // as k_batch_step
     const size_t tile = 2 * 4 * (size_t)(ty + 6) * 40 * es;  // two tile buffers
     const size_t fx = (size_t)ns::batch::kWarps * 2 * 32 * (pw + 1) * es;
     return std::max(tile, fx);
 }
 
-template <typename T, int TY>
-int occupancy(size_t smem)
+int occupancy(StepKernel k, size_t smem)
 {
     int nb = 0;
-    cudaFuncSetAttribute(ns::batch::k_batch_step<T, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, ns::batch::k_batch_step<T, TY>, 256, smem);
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, 256, smem);
     return nb;
 }
 
-int configure(ns_batch *b, int ty, int bps)
+int configure(ns_batch *b, int ty, int pw, int bps)
 {
     int nsm = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, b->dev);
     b->ty = ty;
-    b->smem = smem_for(b->precision, ty);
-    int maxb = b->precision == NS_PREC_SPLIT32
-                   ? (ty == 8 ? occupancy<float, 8>(b->smem) : occupancy<float, 16>(b->smem))
-                   : (ty == 8 ? occupancy<double, 8>(b->smem) : occupancy<double, 16>(b->smem));
+    b->pw = pw;
+    b->smem = smem_for(b->precision, ty, pw);
+    const int maxb = occupancy(step_kernel(b->precision, ty, pw), b->smem);
     if (maxb < 1) return berr(b, NS_ERR_CUDA, "ns_batch: the step kernel cannot be resident");
     b->blocks_per_sm = (bps > 0 && bps < maxb) ? bps : maxb;
     b->grid = b->blocks_per_sm * nsm;
@@ -1414,7 +1421,7 @@ int ns_batch_create(const ns_params *const *params, int n, int precision, ns_bat
         a.err = b->err;
         a.spin_limit = 20000000;  // x 64 ns sleeps: about 1-2 s per barrier
     }
-    rc = configure(b, 16, 0);
+    rc = configure(b, 16, 16, 0);
     if (rc != NS_OK) goto fail;
 #undef B_TRY
     *out = b;
@@ -1592,15 +1599,16 @@ int ns_batch_autotune(ns_batch *b, int iter0, int reps, int *ty, int *blocks_per
     if (!b->have_state) return berr(b, NS_ERR_STATE, "ns_batch_autotune before ns_batch_set_state");
     cudaSetDevice(b->dev);
     double best = 1e300;
-    int bty = 16, bbps = 0;
+    int bty = 16, bpw = 16, bbps = 0;
     int it = iter0;
-    for (int t : {8, 16}) {
-        const size_t sm = smem_for(b->precision, t);
-        const int maxb = b->precision == NS_PREC_SPLIT32
-                             ? (t == 8 ? occupancy<float, 8>(sm) : occupancy<float, 16>(sm))
-                             : (t == 8 ? occupancy<double, 8>(sm) : occupancy<double, 16>(sm));
+    const bool f32 = b->precision == NS_PREC_SPLIT32;
+    for (int t : {8, 16})
+    for (int pw : {16, 24, 32}) {
+        if (!f32 && pw != 16) continue;  // FP32: 16, 24 or 32; FP64: 16
+        const size_t sm = smem_for(b->precision, t, pw);
+        const int maxb = occupancy(step_kernel(b->precision, t, pw), sm);
         for (int bps = 1; bps <= maxb; bps++) {
-            int rc = configure(b, t, bps);
+            int rc = configure(b, t, pw, bps);
             if (rc != NS_OK) return rc;
             if (!b->no_graph && ensure_graph(b) != NS_OK) b->no_graph = true;
             auto one = [&]() {
@@ -1625,11 +1633,12 @@ int ns_batch_autotune(ns_batch *b, int iter0, int reps, int *ty, int *blocks_per
             if (t_ms / reps < best) {
                 best = t_ms / reps;
                 bty = t;
+                bpw = pw;
                 bbps = bps;
             }
         }
     }
-    int rc = configure(b, bty, bbps);
+    int rc = configure(b, bty, bpw, bbps);
     if (rc != NS_OK) return rc;
     b->tuned_ms = best;
     if (ty) *ty = bty;
@@ -1664,13 +1673,7 @@ int ns_batch_barrier_test(ns_batch *b, int extra, long long spin_limit)
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    cudaError_t e;
-    if (b->precision == NS_PREC_SPLIT32)
-        e = b->ty == 8 ? cudaLaunchKernelEx(&cfg, ns::batch::k_batch_step<float, 8>, a)
-                       : cudaLaunchKernelEx(&cfg, ns::batch::k_batch_step<float, 16>, a);
-    else
-        e = b->ty == 8 ? cudaLaunchKernelEx(&cfg, ns::batch::k_batch_step<double, 8>, a)
-                       : cudaLaunchKernelEx(&cfg, ns::batch::k_batch_step<double, 16>, a);
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, step_kernel(b->precision, b->ty, b->pw), a);
     b->args = saved;
     if (e != cudaSuccess) return berr(b, NS_ERR_CUDA, std::string("ns_batch_barrier_test: ") + cudaGetErrorString(e));
     return ns_batch_synchronize(b);
