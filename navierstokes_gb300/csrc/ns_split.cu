@@ -771,12 +771,16 @@ __global__ void __launch_bounds__(128)
 
 // x filter: each warp owns 32 consecutive rows of one variable and one
 // chunk.  The old values a lane appends to its window (position q+7 at step
-// q) are staged 32 positions at a time through [32][33] tiles: every lane
-// copies position q+7+lane of each row with cp.async (no registers, no
-// wait), the next block's copies issued before the current block is
-// filtered (two tiles per plane).  Step t reads column t of its own row and
-// leaves its output there; the tile then goes back with coalesced row
-// writes.  Pair variables stage their lo parts through a second tile pair.
+// q) are staged kSplitXB positions at a time through [32][kSplitXB+1] tiles
+// (an odd row stride: column reads are free of bank conflicts): lane x
+// copies position q+7+x of each row with cp.async (no registers, no wait),
+// the next block's copies issued before the current block is filtered (two
+// tiles per plane).  Step t reads column t of its own row and leaves its
+// output there; the tile then goes back with coalesced row writes.  Pair
+// variables stage their lo parts through a second tile pair.  The tiles set
+// the shared memory per warp and with it the resident warps: 32 positions
+// take 2 x 2 x 4.2 KB per warp for pairs.
+constexpr int kSplitXB = 32;
 // warps per block: 4 for single FP32 variables, 2 when the lo tiles exist
 template <int NP>
 constexpr int x_warps()
@@ -808,9 +812,10 @@ __device__ __forceinline__ void filter_x_rows(const float *__restrict__ sbase,
                                               float *__restrict__ obase, float *__restrict__ olbase,
                                               int fpitch, int n, int nrows, int lane, int a, int b,
                                               bool exact, bool first, bool last, int q0,
-                                              const FiltF &f, float (*ti)[32][33],
-                                              float (*til)[32][33])
+                                              const FiltF &f, float (*ti)[32][kSplitXB + 1],
+                                              float (*til)[32][kSplitXB + 1])
 {
+    constexpr int XB = kSplitXB;
     const bool active = lane < nrows;
     const long long roff = (long long)(active ? lane : 0) * fpitch;
     const float *__restrict__ s = sbase + roff;
@@ -821,10 +826,11 @@ __device__ __forceinline__ void filter_x_rows(const float *__restrict__ sbase,
         const int pos = qb + 7 + lane;
         const int nb = pos < n ? 4 : 0;
         const int pc = pos < n ? pos : 0;
-        for (int r = 0; r < nrows; r++) {
-            cp_async4(&ti[buf][r][lane], sbase + (long long)r * fpitch + pc, nb);
-            if (PAIR) cp_async4(&til[buf][r][lane], slbase + (long long)r * fpitch + pc, nb);
-        }
+        if (lane < XB)
+            for (int r = 0; r < nrows; r++) {
+                cp_async4(&ti[buf][r][lane], sbase + (long long)r * fpitch + pc, nb);
+                if (PAIR) cp_async4(&til[buf][r][lane], slbase + (long long)r * fpitch + pc, nb);
+            }
         cp_async_commit();
     };
     if (q0 < b) issue(0, q0);
@@ -846,21 +852,21 @@ __device__ __forceinline__ void filter_x_rows(const float *__restrict__ sbase,
                 if (PAIR) olbase[(long long)lane * fpitch + p] = wl[p];
             }
     }
-    // Steps q = q0 .. b-1 in blocks of 32: block B covers steps
-    // [q0+32B, q0+32B+32), appends positions q+7, writes outputs at q.
+    // Steps q = q0 .. b-1 in blocks of XB: block B covers steps
+    // [q0+XB*B, q0+XB*B+XB), appends positions q+7, writes outputs at q.
     int buf = 0;
-    for (int qb = q0; qb < b; qb += 32) {
-        const bool more = qb + 32 < b;
+    for (int qb = q0; qb < b; qb += XB) {
+        const bool more = qb + XB < b;
         if (more) {
-            issue(buf ^ 1, qb + 32);
+            issue(buf ^ 1, qb + XB);
             cp_async_wait<1>();  // this block's copies have landed
         } else {
             cp_async_wait<0>();
         }
         __syncwarp();
-        const int nstep = min(32, b - qb);
-        float(*tb)[33] = ti[buf];
-        float(*tbl)[33] = til[PAIR ? buf : 0];
+        const int nstep = min(XB, b - qb);
+        float(*tb)[XB + 1] = ti[buf];
+        float(*tbl)[XB + 1] = til[PAIR ? buf : 0];
         // one step: output q into the tile column it read, window slides
         auto step = [&](int t) {
             float vh, vl = 0.f;
@@ -919,8 +925,8 @@ __device__ __forceinline__ void split_filter_x_body(Dims d, int fpitch, const fl
 {
     constexpr int kXW = x_warps<NP>();
     constexpr int kXL = NP ? kXW : 1;  // lo tiles only when pairs exist
-    __shared__ float tin[kXW][2][32][33];
-    __shared__ float tinl[kXL][2][32][33];
+    __shared__ float tin[kXW][2][32][kSplitXB + 1];
+    __shared__ float tinl[kXL][2][32][kSplitXB + 1];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int rows32 = (d.jmax + 31) / 32;
     const long long gw = (long long)blockIdx.x * kXW + wid;  // global warp
