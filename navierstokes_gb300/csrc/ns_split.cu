@@ -778,9 +778,14 @@ __global__ void __launch_bounds__(128)
 // tiles per plane).  Step t reads column t of its own row and leaves its
 // output there; the tile then goes back with coalesced row writes.  Pair
 // variables stage their lo parts through a second tile pair.  The tiles set
-// the shared memory per warp and with it the resident warps: 32 positions
-// take 2 x 2 x 4.2 KB per warp for pairs.
-constexpr int kSplitXB = 32;
+// the shared memory per warp and with it the resident warps.  Measured on
+// 4096^2: blocks of 32 positions for pairs (0.38 ms; 24: 0.41, 16: 0.44) and
+// 24 for single FP32 variables (0.18 ms; 32: 0.20, 16: 0.22).
+template <int NP>
+constexpr int x_block()
+{
+    return NP ? 32 : 24;
+}
 // warps per block: 4 for single FP32 variables, 2 when the lo tiles exist
 template <int NP>
 constexpr int x_warps()
@@ -806,16 +811,15 @@ __device__ __forceinline__ void cp_async_wait()
     asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
-template <bool PAIR>
+template <bool PAIR, int XB>
 __device__ __forceinline__ void filter_x_rows(const float *__restrict__ sbase,
                                               const float *__restrict__ slbase,
                                               float *__restrict__ obase, float *__restrict__ olbase,
                                               int fpitch, int n, int nrows, int lane, int a, int b,
                                               bool exact, bool first, bool last, int q0,
-                                              const FiltF &f, float (*ti)[32][kSplitXB + 1],
-                                              float (*til)[32][kSplitXB + 1])
+                                              const FiltF &f, float (*ti)[32][XB + 1],
+                                              float (*til)[32][XB + 1])
 {
-    constexpr int XB = kSplitXB;
     const bool active = lane < nrows;
     const long long roff = (long long)(active ? lane : 0) * fpitch;
     const float *__restrict__ s = sbase + roff;
@@ -925,8 +929,9 @@ __device__ __forceinline__ void split_filter_x_body(Dims d, int fpitch, const fl
 {
     constexpr int kXW = x_warps<NP>();
     constexpr int kXL = NP ? kXW : 1;  // lo tiles only when pairs exist
-    __shared__ float tin[kXW][2][32][kSplitXB + 1];
-    __shared__ float tinl[kXL][2][32][kSplitXB + 1];
+    constexpr int XB = x_block<NP>();
+    __shared__ float tin[kXW][2][32][XB + 1];
+    __shared__ float tinl[kXL][2][32][XB + 1];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int rows32 = (d.jmax + 31) / 32;
     const long long gw = (long long)blockIdx.x * kXW + wid;  // global warp
@@ -952,12 +957,12 @@ __device__ __forceinline__ void split_filter_x_body(Dims d, int fpitch, const fl
     NS_CHECK(err, kChkSplit, n >= 13 && 6 <= a && a <= b && b <= n - 6 && q0 >= 6 && q0 <= a &&
                                  fpitch >= n);
     if (is_pair<NP>(k))
-        filter_x_rows<true>(src + k * fplane + roff, src + (k + 3) * fplane + roff,
+        filter_x_rows<true, XB>(src + k * fplane + roff, src + (k + 3) * fplane + roff,
                             dst + k * fplane + roff, dst + (k + 3) * fplane + roff, fpitch, n,
                             nrows, lane, a, b, exact, c == 0, c == chunks - 1, q0, f, tin[wid],
                             tinl[NP ? wid : 0]);
     else
-        filter_x_rows<false>(src + k * fplane + roff, nullptr, dst + k * fplane + roff, nullptr,
+        filter_x_rows<false, XB>(src + k * fplane + roff, nullptr, dst + k * fplane + roff, nullptr,
                              fpitch, n, nrows, lane, a, b, exact, c == 0, c == chunks - 1, q0, f,
                              tin[wid], tinl[0]);
 }
