@@ -145,11 +145,13 @@ def test_rk_euler_dropin_matches_resident(oracle_mod, nslib):
     assert_parity(U, ref, c.Ub, label="rk_euler drop-in")
 
 
-@pytest.mark.parametrize("precision", ["fp64", "fp64_bands", "euler_bands", "split"])
+@pytest.mark.parametrize("precision", ["fp64", "fp64_bands", "euler_bands", "fp64_2048",
+                                       "split"])
 def test_rk_euler_pinned_host_reads_directly(nslib, precision):
     """ns_rk_euler on page-locked host memory: FP64 copies the host array in
-    row bands and starts stage 0 on the bands that have landed, split
-    precision reads and writes it in place; results equal the pageable
+    row bands and starts stage 0 on the bands that have landed (up to 8; also
+    on 2048 x 2048, where the filter sweeps run as many segments per line),
+    split precision reads and writes it in place; results equal the pageable
     path's bit for bit."""
     import torch
     from navierstokes_gb300 import Solver
@@ -159,6 +161,9 @@ def test_rk_euler_pinned_host_reads_directly(nslib, precision):
     elif precision == "fp64_bands":
         # 3 bands of 72, 72 and 56 rows; Navier-Stokes with psi (nk = 5)
         c, prec = cases.mixing_layer_case(imax=96, jmax=200, D=10), L.NS_PREC_FP64
+    elif precision == "fp64_2048":
+        c = cases.uniform_flow_case(imax=2048, jmax=2048, D=30, vortex_upstream=300)
+        prec = L.NS_PREC_FP64
     elif precision == "euler_bands":
         # 8 bands; Euler (nk = 4) with a source
         c = cases.acoustic_pulse_case(imax=72, jmax=520, nk=4, D=12)
