@@ -127,6 +127,8 @@ void free_all(ns_ctx *c)
     if (c->tail_exec) cudaGraphExecDestroy(c->tail_exec);
     for (cudaEvent_t ev : c->band_ev)
         if (ev) cudaEventDestroy(ev);
+    for (cudaEvent_t ev : c->wb_ev)
+        if (ev) cudaEventDestroy(ev);
     if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     double *bufs[] = {c->U,    c->U2,   c->W,     c->dudm, c->dudn, c->aux,
                       c->Ubase, c->src, c->xcoef, c->ycoef, c->sigx, c->sigy,
@@ -956,9 +958,10 @@ int ns_synchronize(ns_ctx *c)
 // each band is converted to planes as it lands, and stage 0's k_prim and
 // k_first run on the bands already converted (k_first of band b once band
 // b+1 holds its 3-row halo), so the transfer overlaps that work.  The rest
-// of the step is a second captured graph; the result goes back to the host
-// array with one pass of the layout kernel.
-static int rk_euler_banded(ns_ctx *c, double *U, double *hv, int iter)
+// of the step but the last stage's y sweep and ccpml is a second captured
+// graph; those two run in row bands, and each finished band goes back to the
+// host array by a copy engine while the next one is filtered.
+static int rk_euler_banded(ns_ctx *c, double *U, int iter)
 {
     const ns::Dims &d = c->d;
     int rc = capture_graph(c, &c->tail_exec, ns::launch_step_tail, "capture of the step tail");
@@ -967,8 +970,10 @@ static int rk_euler_banded(ns_ctx *c, double *U, double *hv, int iter)
         NS_CUDA(c, cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
         for (cudaEvent_t &ev : c->band_ev)
             NS_CUDA(c, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        for (cudaEvent_t &ev : c->wb_ev)
+            NS_CUDA(c, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
     }
-    constexpr int kMaxBands = 8;
+    constexpr int kMaxBands = ns::kMaxBands;
     const int nb = std::max(1, std::min(kMaxBands, d.jmax / 64));
     const int rows = ((d.jmax + nb - 1) / nb + 7) / 8 * 8;
     // the copies into U2 wait for earlier work on the context's stream
@@ -998,7 +1003,32 @@ static int rk_euler_banded(ns_ctx *c, double *U, double *hv, int iter)
     NS_CUDA(c, ns::launch_rows(c, NS_KC_FIRST, r0[n - 1], nr[n - 1], c->stream));
     c->have_state = true;
     NS_CUDA(c, cudaGraphLaunch(c->tail_exec, c->stream));
-    NS_CUDA(c, ns::launch_soa_to_aos(c->U, hv, d, c->stream));
+    // The last stage's y sweep and ccpml band by band.  Each finished band is
+    // converted to U's own layout in the dudm planes (free once the last
+    // stage's k_update has run) and sent home by a copy engine while the next
+    // band is filtered.  The bands' pieces start their warm-ups at other
+    // points than the whole sweep's, so on grids with more than one band the
+    // result differs from ns_step's at the rounding level.
+    int pb[ns::kMaxBands + 1];
+    const int nwb = ns::bands_for(c, pb);
+    double *stage_aos = c->dudm;
+    for (int b = 0; b < nwb; b++) {
+        NS_CUDA(c, ns::launch_filter_y_band(c, pb[b], pb[b + 1], c->stream));
+        NS_CUDA(c, ns::launch_bc_band(c, pb, nwb, b, c->stream));
+        int q0, q1;
+        ns::band_rows(d, pb, nwb, b, q0, q1);
+        ns::Dims db = d;
+        db.jmax = q1 - q0;
+        NS_CUDA(c, ns::launch_soa_to_aos(c->U + (size_t)q0 * d.pitch, stage_aos + row_elems * q0, db,
+                                         c->stream));
+        NS_CUDA(c, cudaEventRecord(c->wb_ev[b], c->stream));
+        NS_CUDA(c, cudaStreamWaitEvent(c->copy_stream, c->wb_ev[b], 0));
+        NS_CUDA(c, cudaMemcpyAsync(U + row_elems * q0, stage_aos + row_elems * q0,
+                                   row_elems * (q1 - q0) * sizeof(double), cudaMemcpyDeviceToHost,
+                                   c->copy_stream));
+    }
+    NS_CUDA(c, cudaEventRecord(c->wb_ev[ns::kMaxBands], c->copy_stream));
+    NS_CUDA(c, cudaStreamWaitEvent(c->stream, c->wb_ev[ns::kMaxBands], 0));
     NS_CUDA(c, cudaStreamSynchronize(c->stream));
     return check_kernel_err(c);
 }
@@ -1027,7 +1057,7 @@ int ns_rk_euler(ns_ctx *c, double *U, double t, int iter, int nk)
         return rc;
     }
     double *hv = static_cast<double *>(dev_view);
-    if (!c->split) return rk_euler_banded(c, U, hv, iter);
+    if (!c->split) return rk_euler_banded(c, U, iter);
     NS_CUDA(c, ns::launch_aos_to_soa(hv, c->U, c->d, c->stream));
     if (c->split) NS_CUDA(c, ns::launch_split_from_full(c, c->U, c->stream));
     c->have_state = true;

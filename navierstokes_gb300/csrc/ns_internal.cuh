@@ -222,6 +222,7 @@ struct ns_ctx {
     cudaGraphExec_t tail_exec = nullptr;
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t band_ev[9] = {};
+    cudaEvent_t wb_ev[9] = {};  // a row band of the last stage is ready to go home
     cudaStream_t graph_stream = nullptr;
     int launches_per_step = 0;
     std::string err;
@@ -232,15 +233,29 @@ struct ns_ctx {
 namespace ns {
 constexpr int kMaxStepLaunches = 64;
 cudaError_t launch_step(ns_ctx *c, cudaStream_t s);
-// The step without stage 0's k_prim and k_first, and those two kernels over a
-// range of rows (FP64 contexts): ns_rk_euler runs them band by band as the
-// rows arrive from the host.
+// The step without stage 0's k_prim and k_first and without the last
+// stage's y sweep and ccpml, and those kernels over ranges of rows (FP64
+// contexts): ns_rk_euler runs them band by band as the rows arrive from the
+// host and as they leave for it.
 cudaError_t launch_step_tail(ns_ctx *c, cudaStream_t s);
 cudaError_t launch_rows(ns_ctx *c, int cls, int row0, int rows, cudaStream_t s);
 // Launch shape of the segmented filter sweeps (ns_kernels.cu): `seg`
 // pass-2 positions per warp, `blocks` blocks of 128 threads.
 void filter_shape(int nlines, int n, int nk, int warm, int nsm, int kw, long long &seg,
                   unsigned &blocks);
+// The same for len2 pass-2 positions per line.
+void filter_shape_len(int nlines, int len2, int nk, int warm, int nsm, int kw, long long &seg,
+                      unsigned &blocks);
+// ns_rk_euler on a page-locked host array runs its last stage's y sweep and
+// ccpml in row bands and sends each band home while the next is filtered:
+// bands_for gives the number of bands and the pass-2 position bounds
+// pb[0..nb] (band b covers pb[b] .. pb[b+1]-1, rows 0..5 belong to band 0
+// and the last six rows to band nb-1: band_rows).  (ns_kernels.cu)
+constexpr int kMaxBands = 8;
+int bands_for(const ns_ctx *c, int *pb);
+void band_rows(const Dims &d, const int *pb, int nb, int b, int &r0, int &r1);
+cudaError_t launch_filter_y_band(ns_ctx *c, int p0, int p1, cudaStream_t s);
+cudaError_t launch_bc_band(ns_ctx *c, const int *pb, int nb, int b, cudaStream_t s);
 cudaError_t launch_kernel(ns_ctx *c, int cls, int stage, cudaStream_t s);
 int step_sequence(const ns_ctx *c, int *cls, int *stage);
 cudaError_t launch_set_iter(int *d_iter, int iter, cudaStream_t s);

@@ -551,14 +551,16 @@ __device__ __forceinline__ void filter_piece(const double *__restrict__ s, doubl
 template <bool ALONG_Y>
 __global__ void __launch_bounds__(128)
     k_filter(Dims d, const double *__restrict__ src, double *__restrict__ dst, long long seg,
-             int warm, FilterCoef fc, int *err)
+             int warm, FilterCoef fc, int *err, int p0, int len2)
 {
     const int lane = threadIdx.x & 31;
     const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nlines = ALONG_Y ? d.imax : d.jmax;  // lines per variable
     const int gpk = (nlines + 31) >> 5;            // warp-lines per variable
     const int n = ALONG_Y ? d.jmax : d.imax;
-    const int len2 = n - 12;                       // pass-2 positions 6 .. n-7
+    // pass-2 positions p0 .. p0+len2-1: all of them (6 .. n-7), or one row
+    // band of ns_rk_euler's last y sweep
+    NS_CHECK(err, kChkKernels, p0 >= 6 && len2 >= 1 && p0 + len2 <= n - 6);
     const long long total = (long long)gpk * d.nk * len2;
     const long long s0 = wid * seg;
     const long long s1 = s0 + seg < total ? s0 + seg : total;
@@ -575,8 +577,8 @@ __global__ void __launch_bounds__(128)
                 (long long)k * d.plane + (ALONG_Y ? line : (long long)line * d.pitch);
             // the line's last point stays inside plane k
             NS_CHECK(err, kChkKernels, base + (long long)(n - 1) * st < (long long)(k + 1) * d.plane);
-            filter_piece(src + base, dst + base, st, n, 6 + (int)(sp - g * len2),
-                         6 + (int)(e - g * len2), warm, fc, err);
+            filter_piece(src + base, dst + base, st, n, p0 + (int)(sp - g * len2),
+                         p0 + (int)(e - g * len2), warm, fc, err);
         }
         sp = e;
     }
@@ -591,8 +593,13 @@ __global__ void __launch_bounds__(128)
 void filter_shape(int nlines, int n, int nk, int warm, int nsm, int kw, long long &seg,
                   unsigned &blocks)
 {
+    filter_shape_len(nlines, n - 12, nk, warm, nsm, kw, seg, blocks);
+}
+
+void filter_shape_len(int nlines, int len2, int nk, int warm, int nsm, int kw, long long &seg,
+                      unsigned &blocks)
+{
     const long long gtot = (long long)nk * ((nlines + 31) / 32);
-    const int len2 = n - 12;
     const long long total = gtot * len2;
     const long long S = 4LL * nsm;
     long long nw;
@@ -638,15 +645,18 @@ __device__ __forceinline__ void bc_column_values(const double *__restrict__ U, c
 // blockIdx.y picks the edge: 0 left, 1 right (rows t), 2 top, 3 bottom
 // (columns t).  The four write disjoint locations and read only points no
 // edge writes, so they run side by side, one memory round trip each.
+// Rows r0 .. r1-1 only (the whole grid but in ns_rk_euler's banded last
+// stage): the left and right edges of those rows, the top row if r1 = jmax,
+// the bottom row if r0 = 0.
 __global__ void k_bc(Dims d, double *__restrict__ U, const double *__restrict__ rhob,
-                     const double *__restrict__ psib, double gamma)
+                     const double *__restrict__ psib, double gamma, int r0, int r1)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int edge = blockIdx.y;
     const long long P = d.plane;
     double v[kMaxNk];
     if (edge < 2) {
-        if (t > 0 && t < d.jmax - 1) {
+        const int t = r0 + blockIdx.x * blockDim.x + threadIdx.x;
+        if (t > 0 && t < d.jmax - 1 && t < r1) {
             const long long r = (long long)t * d.pitch;
             const int i = edge == 0 ? 0 : d.imax - 1;
             bc_column_values(U, d, i, t, rhob, psib, gamma, v);
@@ -654,8 +664,9 @@ __global__ void k_bc(Dims d, double *__restrict__ U, const double *__restrict__ 
         }
         return;
     }
-    if (t >= d.imax) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const bool top = edge == 2;
+    if (t >= d.imax || (top ? r1 != d.jmax : r0 != 0)) return;
     // top (cc.f90:39-43) from rows jt-1, jt-2; bottom (cc.f90:55-59) from rows 1, 2
     const int jt = d.jmax - 1;
     const int j1 = top ? jt - 1 : 1, j2 = top ? jt - 2 : 2, jw = top ? jt : 0;
@@ -787,6 +798,49 @@ cudaError_t launch_rows(ns_ctx *c, int cls, int row0, int rows, cudaStream_t s)
 }
 
 // One kernel of class `cls` (NS_KC_*) for `stage`.
+int bands_for(const ns_ctx *c, int *pb)
+{
+    // as many bands (at most kMaxBands) as keep every band's per-warp
+    // segments at least four warm-ups long (one warp per SM sub-partition):
+    // 8 on 4096 x 2048, 1 on 512 x 512 and smaller grids.  Band b covers
+    // pass-2 positions pb[b] .. pb[b+1]-1.
+    const Dims &d = c->d;
+    const long long total = (long long)d.nk * ((d.imax + 31) / 32) * (d.jmax - 12);
+    const long long per_band = 4LL * c->nsm * 4 * (c->warm + 6);
+    const int nb =
+        c->warm < 0 ? 1 : (int)std::max(1LL, std::min<long long>(kMaxBands, total / per_band));
+    const int len2 = d.jmax - 12;
+    for (int b = 0; b <= nb; b++) pb[b] = 6 + (int)((long long)b * len2 / nb);
+    return nb;
+}
+
+void band_rows(const Dims &d, const int *pb, int nb, int b, int &r0, int &r1)
+{
+    r0 = b == 0 ? 0 : pb[b];
+    r1 = b == nb - 1 ? d.jmax : pb[b + 1];
+}
+
+cudaError_t launch_filter_y_band(ns_ctx *c, int p0, int p1, cudaStream_t s)
+{
+    const Dims &d = c->d;
+    long long seg;
+    unsigned nb;
+    filter_shape_len(d.imax, p1 - p0, d.nk, c->warm, c->nsm, kFilterWarpsPerSmsp, seg, nb);
+    k_filter<true><<<nb, 128, 0, s>>>(d, c->U2, c->U, seg, c->warm, c->fy, c->d_err, p0, p1 - p0);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bc_band(ns_ctx *c, const int *pb, int nb, int b, cudaStream_t s)
+{
+    const Dims &d = c->d;
+    int r0, r1;
+    band_rows(d, pb, nb, b, r0, r1);
+    const int nt = std::max(r1 - r0, d.imax);
+    k_bc<<<dim3((nt + 127) / 128, 4), 128, 0, s>>>(d, c->U, c->rhob, c->psib, c->phys.gamma, r0,
+                                                   r1);
+    return cudaGetLastError();
+}
+
 template <bool VISC, int NK>
 static cudaError_t launch_kernel_t(ns_ctx *c, int cls, int stage, cudaStream_t s)
 {
@@ -828,19 +882,22 @@ static cudaError_t launch_kernel_t(ns_ctx *c, int cls, int stage, cudaStream_t s
         long long seg;
         unsigned nb;
         filter_shape(d.jmax, d.imax, d.nk, c->warm, c->nsm, kFilterWarpsPerSmsp, seg, nb);
-        k_filter<false><<<nb, 128, 0, s>>>(d, c->U, c->U2, seg, c->warm, c->fx, c->d_err);
+        k_filter<false><<<nb, 128, 0, s>>>(d, c->U, c->U2, seg, c->warm, c->fx, c->d_err, 6,
+                                            d.imax - 12);
         break;
     }
     case NS_KC_FILTER_Y: {
         long long seg;
         unsigned nb;
         filter_shape(d.imax, d.jmax, d.nk, c->warm, c->nsm, kFilterWarpsPerSmsp, seg, nb);
-        k_filter<true><<<nb, 128, 0, s>>>(d, c->U2, c->U, seg, c->warm, c->fy, c->d_err);
+        k_filter<true><<<nb, 128, 0, s>>>(d, c->U2, c->U, seg, c->warm, c->fy, c->d_err, 6,
+                                           d.jmax - 12);
         break;
     }
     case NS_KC_BC: {
         const int nt = d.imax > d.jmax ? d.imax : d.jmax;
-        k_bc<<<dim3((nt + 127) / 128, 4), 128, 0, s>>>(d, c->U, c->rhob, c->psib, c->phys.gamma);
+        k_bc<<<dim3((nt + 127) / 128, 4), 128, 0, s>>>(d, c->U, c->rhob, c->psib, c->phys.gamma,
+                                                       0, d.jmax);
         break;
     }
     case NS_KC_STAGE_SIN: {
@@ -902,6 +959,7 @@ cudaError_t launch_step_tail(ns_ctx *c, cudaStream_t s)
     const int n = step_sequence(c, cls, stage);
     for (int q = 0; q < n; q++) {
         if (stage[q] == 0 && (cls[q] == NS_KC_PRIM || cls[q] == NS_KC_FIRST)) continue;
+        if (stage[q] == 5 && (cls[q] == NS_KC_FILTER_Y || cls[q] == NS_KC_BC)) continue;
         cudaError_t e = launch_kernel(c, cls[q], stage[q], s);
         if (e != cudaSuccess) return e;
     }

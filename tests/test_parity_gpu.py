@@ -149,10 +149,12 @@ def test_rk_euler_dropin_matches_resident(oracle_mod, nslib):
                                        "split"])
 def test_rk_euler_pinned_host_reads_directly(nslib, precision):
     """ns_rk_euler on page-locked host memory: FP64 copies the host array in
-    row bands and starts stage 0 on the bands that have landed (up to 8; also
-    on 2048 x 2048, where the filter sweeps run as many segments per line),
-    split precision reads and writes it in place; results equal the pageable
-    path's bit for bit."""
+    row bands and starts stage 0 on the bands that have landed; on grids large
+    enough (2048 x 2048: 4 bands) it also runs the last stage's y sweep and
+    ccpml in row bands and sends each band home while the next is filtered;
+    split precision reads and writes the array in place.  Results equal the
+    pageable path's bit for bit, or to rounding where the last stage is
+    banded."""
     import torch
     from navierstokes_gb300 import Solver
     from navierstokes_gb300 import _lib as L
@@ -181,8 +183,14 @@ def test_rk_euler_pinned_host_reads_directly(nslib, precision):
     with Solver(c, precision=prec) as s:
         for it in range(4):
             s.rk_euler(paged, (it + 1) * c.dt, it)
-    assert np.array_equal(pinned, paged)
     assert not np.array_equal(pinned, c.U0)
+    if precision != "fp64_2048":
+        assert np.array_equal(pinned, paged)
+    else:
+        # 2048 x 2048 runs the last stage's y sweep in row bands on the pinned
+        # path: its pieces warm up from other points than the whole sweep's,
+        # so the two agree to rounding
+        assert_parity(pinned, paged, c.Ub, tol=1e-14, label="banded last stage")
 
 
 def test_rk_euler_on_registered_host_array(nslib):
