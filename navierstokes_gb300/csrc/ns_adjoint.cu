@@ -199,6 +199,18 @@ __device__ __forceinline__ void transpose13(const FilterCoef &fc, double *w)
     w[6] = fc.c0 * lq;
 }
 
+// The same in FP32 (the first steps of a warm start); cf = c0, m[1..6].
+__device__ __forceinline__ void transpose13_f(const float *cf, float *w)
+{
+    const float lq = w[6];
+#pragma unroll
+    for (int s = 1; s <= 6; s++) {
+        w[6 - s] = fmaf(cf[s], lq, w[6 - s]);
+        w[6 + s] = fmaf(cf[s], lq, w[6 + s]);
+    }
+    w[6] = cf[0] * lq;
+}
+
 // Slides the window one point down; `next` is the untouched adjoint at q-7.
 __device__ __forceinline__ void shift13_down(double *w, double next)
 {
@@ -209,12 +221,12 @@ __device__ __forceinline__ void shift13_down(double *w, double next)
 
 // Pass-2 positions [a, b) of one line, transposed: b == n-6 starts exactly
 // with pass 3^T at the top, a later end runs `warm` points of history
-// first (or starts exactly when that reaches the top); a == 6 ends with
-// pass 1^T.  Writes positions a+6 .. b+5 (and 0..11 when a == 6, the top
-// when b == n-6).
+// first, the first warm32 of them in FP32 (or starts exactly when that
+// reaches the top); a == 6 ends with pass 1^T.  Writes positions
+// a+6 .. b+5 (and 0..11 when a == 6, the top when b == n-6).
 __device__ __forceinline__ void filter_piece_t(const double *__restrict__ s, double *__restrict__ o,
                                                long long st, int n, int a, int b, int warm,
-                                               const FilterCoef &fc)
+                                               int warm32, const FilterCoef &fc)
 {
     double w[13];
     int q;
@@ -238,8 +250,22 @@ __device__ __forceinline__ void filter_piece_t(const double *__restrict__ s, dou
         q = qtop;
     } else {
         q = b - 1 + warm;
+        // the untouched history's error decays below the FP32 rounding in the
+        // first warm32 steps, which therefore run in FP32 (no outputs there)
+        float wf[13], cf[7];
+        cf[0] = (float)fc.c0;
 #pragma unroll
-        for (int t = 0; t < 13; t++) w[t] = s[(long long)(q - 6 + t) * st];
+        for (int z = 1; z < 7; z++) cf[z] = (float)fc.m[z];
+#pragma unroll
+        for (int t = 0; t < 13; t++) wf[t] = (float)s[(long long)(q - 6 + t) * st];
+        for (const int qe = q - warm32; q > qe; q--) {
+            transpose13_f(cf, wf);
+#pragma unroll
+            for (int t = 12; t > 0; t--) wf[t] = wf[t - 1];
+            wf[0] = (float)s[(long long)(q - 7) * st];
+        }
+#pragma unroll
+        for (int t = 0; t < 13; t++) w[t] = (double)wf[t];
     }
     // blocks of kFilterPf points, the next block's input loaded ahead
     double nx[kFilterPf];
@@ -289,7 +315,7 @@ __device__ __forceinline__ void filter_piece_t(const double *__restrict__ s, dou
 template <bool ALONG_Y>
 __global__ void __launch_bounds__(128)
     k_filter_t(Dims d, const double *__restrict__ in, double *__restrict__ out, long long seg,
-               int warm, FilterCoef fc)
+               int warm, int warm32, FilterCoef fc)
 {
     const int lane = threadIdx.x & 31;
     const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -311,7 +337,7 @@ __global__ void __launch_bounds__(128)
             const long long base =
                 (long long)k * d.plane + (ALONG_Y ? line : (long long)line * d.pitch);
             filter_piece_t(in + base, out + base, st, n, 6 + (int)(sp - g * len2),
-                           6 + (int)(e - g * len2), warm, fc);
+                           6 + (int)(e - g * len2), warm, warm32, fc);
         }
         sp = e;
     }
@@ -595,9 +621,11 @@ int stage_adjoint(ns_adjoint *a, const double *U, const double *Um, const double
         long long seg;
         unsigned nb;
         ns::filter_shape(d.imax, d.jmax, 4, c->warm, c->nsm, ns::kFilterWarpsPerSmsp, seg, nb);
-        ns::adj::k_filter_t<true><<<nb, 128, 0, s>>>(d, a->lam, a->lam2, seg, c->warm, c->fy);
+        ns::adj::k_filter_t<true><<<nb, 128, 0, s>>>(d, a->lam, a->lam2, seg, c->warm, c->warm32,
+                                                      c->fy);
         ns::filter_shape(d.jmax, d.imax, 4, c->warm, c->nsm, ns::kFilterWarpsPerSmsp, seg, nb);
-        ns::adj::k_filter_t<false><<<nb, 128, 0, s>>>(d, a->lam2, a->lam, seg, c->warm, c->fx);
+        ns::adj::k_filter_t<false><<<nb, 128, 0, s>>>(d, a->lam2, a->lam, seg, c->warm, c->warm32,
+                                                       c->fx);
     }
     const dim3 blk(32, 8), grd((d.imax + 31) / 32, (d.jmax + 7) / 8);
     ns::adj::k_point_t<<<grd, blk, 0, s>>>(d, a->lam, a->om, a->lx, a->ly, U, Um, Un,

@@ -812,7 +812,7 @@ constants:
             c->alpha[k] = kAlpha[k];
             c->beta[k] = kBeta[k];
         }
-        c->warm = warmup(p->sigmaf, std::ldexp(1.0, -60), 36);
+        fp64_warmups(p->sigmaf, c->warm, c->warm32);
         int nsm = 152;
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->dev);
         c->nsm = nsm;

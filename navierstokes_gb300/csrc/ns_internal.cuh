@@ -210,6 +210,7 @@ struct ns_ctx {
     ns::FilterCoef fx, fy;
     double ct[6], alpha[6], beta[6];
     int warm = 0;       // filter warm-up length (-1: serial sweeps)
+    int warm32 = 0;     // its first warm32 steps run in FP32 (ns_coef.h fp64_warmups)
     int nsm = 152;      // multiprocessors of the device
     bool visc = false;
     bool split = false;

@@ -461,13 +461,28 @@ __device__ __forceinline__ void shift13(double *w, double v, double next)
     w[12] = next;
 }
 
+// The pass-2 point of filter13 in FP32 (the first steps of a warm start);
+// cf = c0, m[1..6] rounded to FP32.
+__device__ __forceinline__ float filter13_f(const float *cf, const float *w)
+{
+    float v = cf[0] * w[6];
+    v = fmaf(cf[6], w[12] + w[0], v);
+    v = fmaf(cf[5], w[11] + w[1], v);
+    v = fmaf(cf[4], w[10] + w[2], v);
+    v = fmaf(cf[3], w[9] + w[3], v);
+    v = fmaf(cf[2], w[8] + w[4], v);
+    v = fmaf(cf[1], w[7], v);
+    return fmaf(cf[1], w[5], v);
+}
+
 // Pass-2 positions [a, b) of one line (6 <= a < b <= n-6): a == 6 starts
 // exactly with pass 1 and writes its outputs, a later start runs `warm`
 // points of unfiltered history first (or starts exactly when that reaches
-// back to position 6); b == n-6 ends with pass 3.
+// back to position 6), the first warm32 of them in FP32; b == n-6 ends with
+// pass 3.
 __device__ __forceinline__ void filter_piece(const double *__restrict__ s, double *__restrict__ o,
                                              long long st, int n, int a, int b, int warm,
-                                             const FilterCoef &fc, int *err)
+                                             int warm32, const FilterCoef &fc, int *err)
 {
     // positions read: 0..12 (exact start) or a-warm-6 .. , ahead up to n-1;
     // written: a .. b-1 and the pass-1/pass-3 ends
@@ -493,8 +508,26 @@ __device__ __forceinline__ void filter_piece(const double *__restrict__ s, doubl
         q = 6;
     } else {
         q = a - warm;
+        // the history's own error decays below the FP32 rounding in the
+        // first warm32 steps, which therefore run in FP32; the FP64 steps
+        // after them take that rounding below 2^-60
+        float wf[13], cf[7];
+        cf[0] = (float)fc.c0;
 #pragma unroll
-        for (int t = 0; t < 13; t++) w[t] = s[(long long)(q - 6 + t) * st];
+        for (int z = 1; z < 7; z++) cf[z] = (float)fc.m[z];
+#pragma unroll
+        for (int t = 0; t < 13; t++) wf[t] = (float)s[(long long)(q - 6 + t) * st];
+        for (const int qe = q + warm32; q < qe; q++) {
+            const float v = filter13_f(cf, wf);
+#pragma unroll
+            for (int t = 0; t < 5; t++) wf[t] = wf[t + 1];
+            wf[5] = v;
+#pragma unroll
+            for (int t = 6; t < 12; t++) wf[t] = wf[t + 1];
+            wf[12] = (float)s[(long long)(q + 7) * st];
+        }
+#pragma unroll
+        for (int t = 0; t < 13; t++) w[t] = (double)wf[t];
     }
     // pass 2 (filtering.f90:69-79 / :161-171).  Blocks of kFilterPf points,
     // the next block's input loaded before the current block is filtered, so
@@ -551,7 +584,7 @@ __device__ __forceinline__ void filter_piece(const double *__restrict__ s, doubl
 template <bool ALONG_Y>
 __global__ void __launch_bounds__(128)
     k_filter(Dims d, const double *__restrict__ src, double *__restrict__ dst, long long seg,
-             int warm, FilterCoef fc, int *err, int p0, int len2)
+             int warm, int warm32, FilterCoef fc, int *err, int p0, int len2)
 {
     const int lane = threadIdx.x & 31;
     const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -578,7 +611,7 @@ __global__ void __launch_bounds__(128)
             // the line's last point stays inside plane k
             NS_CHECK(err, kChkKernels, base + (long long)(n - 1) * st < (long long)(k + 1) * d.plane);
             filter_piece(src + base, dst + base, st, n, p0 + (int)(sp - g * len2),
-                         p0 + (int)(e - g * len2), warm, fc, err);
+                         p0 + (int)(e - g * len2), warm, warm32, fc, err);
         }
         sp = e;
     }
@@ -826,7 +859,7 @@ cudaError_t launch_filter_y_band(ns_ctx *c, int p0, int p1, cudaStream_t s)
     long long seg;
     unsigned nb;
     filter_shape_len(d.imax, p1 - p0, d.nk, c->warm, c->nsm, kFilterWarpsPerSmsp, seg, nb);
-    k_filter<true><<<nb, 128, 0, s>>>(d, c->U2, c->U, seg, c->warm, c->fy, c->d_err, p0, p1 - p0);
+    k_filter<true><<<nb, 128, 0, s>>>(d, c->U2, c->U, seg, c->warm, c->warm32, c->fy, c->d_err, p0, p1 - p0);
     return cudaGetLastError();
 }
 
@@ -882,7 +915,7 @@ static cudaError_t launch_kernel_t(ns_ctx *c, int cls, int stage, cudaStream_t s
         long long seg;
         unsigned nb;
         filter_shape(d.jmax, d.imax, d.nk, c->warm, c->nsm, kFilterWarpsPerSmsp, seg, nb);
-        k_filter<false><<<nb, 128, 0, s>>>(d, c->U, c->U2, seg, c->warm, c->fx, c->d_err, 6,
+        k_filter<false><<<nb, 128, 0, s>>>(d, c->U, c->U2, seg, c->warm, c->warm32, c->fx, c->d_err, 6,
                                             d.imax - 12);
         break;
     }
@@ -890,7 +923,7 @@ static cudaError_t launch_kernel_t(ns_ctx *c, int cls, int stage, cudaStream_t s
         long long seg;
         unsigned nb;
         filter_shape(d.imax, d.jmax, d.nk, c->warm, c->nsm, kFilterWarpsPerSmsp, seg, nb);
-        k_filter<true><<<nb, 128, 0, s>>>(d, c->U2, c->U, seg, c->warm, c->fy, c->d_err, 6,
+        k_filter<true><<<nb, 128, 0, s>>>(d, c->U2, c->U, seg, c->warm, c->warm32, c->fy, c->d_err, 6,
                                            d.jmax - 12);
         break;
     }

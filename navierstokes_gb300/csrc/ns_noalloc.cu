@@ -278,7 +278,7 @@ extern "C" int ns_step_noalloc(const ns_params *p, double *U, int64_t pitch, int
         c.alpha[k] = kAlpha[k];
         c.beta[k] = kBeta[k];
     }
-    c.warm = warmup(p->sigmaf, std::ldexp(1.0, -60), 36);
+    fp64_warmups(p->sigmaf, c.warm, c.warm32);
     int nsm = 152;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     c.nsm = nsm;
