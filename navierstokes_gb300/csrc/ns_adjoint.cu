@@ -22,7 +22,10 @@
 #include <string>
 #include <vector>
 
+#include "ns_check.cuh"
+#include "ns_coef.h"
 #include "ns_internal.cuh"
+#include "ns_tma.cuh"
 
 namespace ns {
 namespace adj {
@@ -445,41 +448,79 @@ __device__ __forceinline__ double dcoef(const double *tab, int r, int q, int n)
     return (z >= 0 && z < 7) ? c[z] : 0.0;
 }
 
+// sum_r D[r][q] * g[r] at a point q in [9, n-9), whose neighbours within 6
+// are interior rows (no closure row reaches it): g in global or shared memory
+__device__ __forceinline__ double dtrans_int(const double *g, long long st, int q,
+                                             const double *__restrict__ tab)
+{
+    double r = 0.0;
+#pragma unroll
+    for (int s = 1; s <= 3; s++) {
+        r = fma(tab[kCoefStride * (q - s) + 3 + s], g[-s * st], r);
+        r = fma(-tab[kCoefStride * (q + s) + 3 + s], g[s * st], r);
+    }
+    return r;
+}
+
 // sum_r D[r][q] * g[r] along one line
 __device__ __forceinline__ double dtrans(const double *__restrict__ g, long long st, int q, int n,
                                          const double *__restrict__ tab)
 {
-    if (q >= 9 && q < n - 9) {
-        const double *t = tab;
-        double r = 0.0;
-#pragma unroll
-        for (int s = 1; s <= 3; s++) {
-            r = fma(t[kCoefStride * (q - s) + 3 + s], g[-s * st], r);
-            r = fma(-t[kCoefStride * (q + s) + 3 + s], g[s * st], r);
-        }
-        return r;
-    }
+    if (q >= 9 && q < n - 9) return dtrans_int(g, st, q, tab);
     double r = 0.0;
     for (int rr = max(0, q - 6); rr <= min(n - 1, q + 6); rr++)
         r = fma(dcoef(tab, rr, q, n), g[(long long)(rr - q) * st], r);
     return r;
 }
 
-// lam += Dx^T lx + Dy^T ly
+// Block and tiles of k_deriv_t: 32 x 8 points; lx with its x halo (box
+// 40 x 8 x 4 from (i0-4, j0): the x coordinate times 8 bytes stays a
+// multiple of 16) and ly with its y halo (box 32 x 14 x 4 from (i0, j0-3)).
+constexpr int kDtBX = 32, kDtBY = 8, kDtXW = 40, kDtXL = 4, kDtYH = kDtBY + 6;
+
+// lam += Dx^T lx + Dy^T ly.  With TMA both tiles arrive in shared memory by
+// one bulk copy each and the interior gathers read them there; points within
+// 9 of an edge (closure rows reach them) read global memory.  Both give
+// identical bits.
+template <bool TMA>
 __global__ void __launch_bounds__(256)
-    k_deriv_t(Dims d, double *__restrict__ lam, const double *__restrict__ lx,
-              const double *__restrict__ ly, const double *__restrict__ xcoef,
-              const double *__restrict__ ycoef)
+    k_deriv_t(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap ymap,
+              int *__restrict__ err, Dims d, double *__restrict__ lam,
+              const double *__restrict__ lx, const double *__restrict__ ly,
+              const double *__restrict__ xcoef, const double *__restrict__ ycoef)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    __shared__ alignas(128) double sx[TMA ? 4 : 1][TMA ? kDtBY : 1][TMA ? kDtXW : 1];
+    __shared__ alignas(128) double sy[TMA ? 4 : 1][TMA ? kDtYH : 1][TMA ? kDtBX : 1];
+    __shared__ alignas(8) unsigned long long tbar;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int i = blockIdx.x * kDtBX + tx;
+    const int j = blockIdx.y * kDtBY + ty;
+    NS_CHECK(err, kChkAdjoint, blockDim.x == kDtBX && blockDim.y == kDtBY);
+    if constexpr (TMA) {
+        const bool lead = (tx == 0 && ty == 0);
+        if (lead) mbar_init(&tbar, 1);
+        __syncthreads();
+        if (lead) {
+            const int i0 = blockIdx.x * kDtBX, j0 = blockIdx.y * kDtBY;
+            mbar_expect_tx(&tbar, (unsigned)(sizeof(sx) + sizeof(sy)));
+            tma_load_3d(&sx[0][0][0], &xmap, i0 - kDtXL, j0, 0, &tbar);
+            tma_load_3d(&sy[0][0][0], &ymap, i0, j0 - 3, 0, &tbar);
+        }
+        if (!mbar_wait_bounded(&tbar, 0, err)) return;
+    }
     if (i >= d.imax || j >= d.jmax) return;
     const long long idx = (long long)j * d.pitch + i, P = d.plane;
+    const bool xin = TMA && i >= 9 && i < d.imax - 9;
+    const bool yin = TMA && j >= 9 && j < d.jmax - 9;
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-        const double v = dtrans(lx + k * P + idx, 1, i, d.imax, xcoef) +
-                         dtrans(ly + k * P + idx, d.pitch, j, d.jmax, ycoef);
-        lam[k * P + idx] += v;
+        const double vx = xin ? dtrans_int(&sx[TMA ? k : 0][TMA ? ty : 0][TMA ? tx + kDtXL : 0], 1,
+                                           i, xcoef)
+                              : dtrans(lx + k * P + idx, 1, i, d.imax, xcoef);
+        const double vy = yin ? dtrans_int(&sy[TMA ? k : 0][TMA ? ty + 3 : 0][TMA ? tx : 0], kDtBX,
+                                           j, ycoef)
+                              : dtrans(ly + k * P + idx, d.pitch, j, d.jmax, ycoef);
+        lam[k * P + idx] += vx + vy;
     }
 }
 
@@ -517,6 +558,9 @@ struct ns_adjoint {
     double *lam = nullptr, *lam2 = nullptr, *om = nullptr, *lx = nullptr, *ly = nullptr;
     double *gS = nullptr;
     double *dudm0 = nullptr, *dudn0 = nullptr;  // the context's own derivative planes
+    CUtensorMap lxmap{}, lymap{};  // k_deriv_t's tiles of lx and ly
+    bool dt_maps = false;
+    int warm_t = -1, warm32_t = 0;  // warm-ups of the transposed filter sweeps
     double sin_host[6];
     bool forward_done = false;
     std::string err;
@@ -620,18 +664,23 @@ int stage_adjoint(ns_adjoint *a, const double *U, const double *Um, const double
     {
         long long seg;
         unsigned nb;
-        ns::filter_shape(d.imax, d.jmax, 4, c->warm, c->nsm, ns::kFilterWarpsPerSmsp, seg, nb);
-        ns::adj::k_filter_t<true><<<nb, 128, 0, s>>>(d, a->lam, a->lam2, seg, c->warm, c->warm32,
-                                                      c->fy);
-        ns::filter_shape(d.jmax, d.imax, 4, c->warm, c->nsm, ns::kFilterWarpsPerSmsp, seg, nb);
-        ns::adj::k_filter_t<false><<<nb, 128, 0, s>>>(d, a->lam2, a->lam, seg, c->warm, c->warm32,
-                                                       c->fx);
+        ns::filter_shape(d.imax, d.jmax, 4, a->warm_t, c->nsm, ns::kFilterWarpsPerSmsp, seg, nb);
+        ns::adj::k_filter_t<true><<<nb, 128, 0, s>>>(d, a->lam, a->lam2, seg, a->warm_t,
+                                                      a->warm32_t, c->fy);
+        ns::filter_shape(d.jmax, d.imax, 4, a->warm_t, c->nsm, ns::kFilterWarpsPerSmsp, seg, nb);
+        ns::adj::k_filter_t<false><<<nb, 128, 0, s>>>(d, a->lam2, a->lam, seg, a->warm_t,
+                                                       a->warm32_t, c->fx);
     }
     const dim3 blk(32, 8), grd((d.imax + 31) / 32, (d.jmax + 7) / 8);
     ns::adj::k_point_t<<<grd, blk, 0, s>>>(d, a->lam, a->om, a->lx, a->ly, U, Um, Un,
                                            c->sigx, c->sigy, a->gS, c->phys.gamma, c->p.dt,
                                            c->alpha[stage], c->beta[stage], sink);
-    ns::adj::k_deriv_t<<<grd, blk, 0, s>>>(d, a->lam, a->lx, a->ly, c->xcoef, c->ycoef);
+    if (a->dt_maps)
+        ns::adj::k_deriv_t<true><<<grd, blk, 0, s>>>(a->lxmap, a->lymap, c->d_err, d, a->lam, a->lx,
+                                                     a->ly, c->xcoef, c->ycoef);
+    else
+        ns::adj::k_deriv_t<false><<<grd, blk, 0, s>>>(a->lxmap, a->lymap, c->d_err, d, a->lam,
+                                                      a->lx, a->ly, c->xcoef, c->ycoef);
     A_CUDA(a, cudaGetLastError());
     return NS_OK;
 }
@@ -733,6 +782,12 @@ int ns_adjoint_create(const ns_params *p, int nobs, const double *obs_x, const d
     ns_ctx *c = a->fwd;
     a->K = checkpoint_every;
     a->nobs = nobs;
+    // The transposed sweeps' pieces warm up until the error of their
+    // unfiltered start is below 2^-50 of the data (the forward sweeps: 2^-60,
+    // rounding-level agreement with the serial sweep): about 1e-15 per sweep,
+    // far below the 1e-9 to which a gradient is compared with finite
+    // differences, and 5 FP64 steps fewer per piece at sigmaf = 0.2.
+    ns::coef::fp64_warmups(p->sigmaf, a->warm_t, a->warm32_t, 50);
     a->dudm0 = c->dudm;
     a->dudn0 = c->dudn;
     // base pressure (uniform p_b is required: the loss is on p - p_b)
@@ -770,6 +825,11 @@ int ns_adjoint_create(const ns_params *p, int nobs, const double *obs_x, const d
         ns_adjoint_destroy(a);
         return rc;
     }
+    // the tiled transposed derivative when the context's FP64 tiles are in
+    // use (same layout); otherwise every point reads global memory
+    a->dt_maps = c->fp64_maps &&
+                 ns::make_plane_map(c, &a->lxmap, a->lx, 4, ns::adj::kDtXW, ns::adj::kDtBY) == NS_OK &&
+                 ns::make_plane_map(c, &a->lymap, a->ly, 4, ns::adj::kDtBX, ns::adj::kDtYH) == NS_OK;
     *out = a;
     return NS_OK;
 }

@@ -252,10 +252,11 @@ int make_split_map(ns_ctx *c, CUtensorMap *map, float *base, int planes)
 }
 
 // TMA map of `depth` planes of pitch x jmax doubles from `base`, box
-// 40 x 14 x planes (the halo tile of the FP64 stage kernels); depth 0 means
-// depth = planes.
+// box_w x box_h x planes (by default 40 x 14, the halo tile of the FP64
+// stage kernels); depth 0 means depth = planes.
 static int make_fp64_map(ns_ctx *c, CUtensorMap *map, double *base, int planes,
-                         int depth = 0)
+                         int depth = 0, int box_w = ns::kFirstTileW,
+                         int box_h = ns::kFirstTileH)
 {
     if (depth == 0) depth = planes;
     const auto encode = tensor_map_encoder();
@@ -264,8 +265,7 @@ static int make_fp64_map(ns_ctx *c, CUtensorMap *map, double *base, int planes,
     const cuuint64_t dims[3] = {(cuuint64_t)d.imax, (cuuint64_t)d.jmax, (cuuint64_t)depth};
     const cuuint64_t strides[2] = {(cuuint64_t)d.pitch * sizeof(double),
                                    (cuuint64_t)d.plane * sizeof(double)};
-    const cuuint32_t box[3] = {(cuuint32_t)ns::kFirstTileW, (cuuint32_t)ns::kFirstTileH,
-                               (cuuint32_t)planes};
+    const cuuint32_t box[3] = {(cuuint32_t)box_w, (cuuint32_t)box_h, (cuuint32_t)planes};
     const cuuint32_t estr[3] = {1u, 1u, 1u};
     const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, base, dims, strides, box,
                               estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
@@ -457,6 +457,11 @@ int create_split(ns_ctx *c)
 
 namespace ns {
 PFN_cuTensorMapEncodeTiled_v12000 tensor_encoder() { return tensor_map_encoder(); }
+
+int make_plane_map(ns_ctx *c, CUtensorMap *map, double *base, int planes, int box_w, int box_h)
+{
+    return make_fp64_map(c, map, base, planes, 0, box_w, box_h);
+}
 
 int check_error(int word)
 {

@@ -118,15 +118,15 @@ inline int warmup(double sigmaf, double thresh, int floor)
 // Warm-up of the FP64 sweeps cut into pieces.  A piece that starts from
 // unfiltered history first runs warm32 steps in FP32, until the response to
 // that history is below 2^-24 (the FP32 rounding), then warm - warm32 steps in
-// FP64, until the response to the FP32 phase's rounding is below 2^-60 of
-// the data: the same bound as an all-FP64 warm-up of 2^-60, with most of the
-// FP64 steps replaced by FP32 ones (for sigmaf = 0.2: 20 FP32 + 28 FP64
-// instead of 44 FP64).  warm = -1 (serial sweeps) when the recurrence does
-// not decay.
-inline void fp64_warmups(double sigmaf, int &warm, int &warm32)
+// FP64, until the response to the FP32 phase's rounding is below
+// 2^-total_bits of the data: the same bound as an all-FP64 warm-up to that
+// level, with most of the FP64 steps replaced by FP32 ones (for sigmaf = 0.2
+// and the forward sweeps' 2^-60: 20 FP32 + 28 FP64 instead of 44 FP64).
+// warm = -1 (serial sweeps) when the recurrence does not decay.
+inline void fp64_warmups(double sigmaf, int &warm, int &warm32, int total_bits = 60)
 {
     const int w32 = warmup(sigmaf, std::ldexp(1.0, -24), 0);
-    const int w64 = warmup(sigmaf, std::ldexp(1.0, -36), 16);
+    const int w64 = warmup(sigmaf, std::ldexp(1.0, 24 - total_bits), 16);
     if (w32 < 0 || w64 < 0) {
         warm = -1;
         warm32 = 0;

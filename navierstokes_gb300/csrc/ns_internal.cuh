@@ -291,6 +291,10 @@ void record_error(const char *msg);
 // cuTensorMapEncodeTiled through the runtime's driver entry point, or null
 // when it is unavailable (ns_api.cu).
 PFN_cuTensorMapEncodeTiled_v12000 tensor_encoder();
+// TMA map of `planes` planes of the context's pitch x jmax FP64 layout from
+// `base`, box box_w x box_h x planes (ns_api.cu); NS_OK or the error code
+// set on the context.
+int make_plane_map(ns_ctx *c, CUtensorMap *map, double *base, int planes, int box_w, int box_h);
 // NS_ERR_CHECK for an error word a failed index check of the checked build
 // left (ns_check.cuh), with the file and line as the error text (ns_api.cu).
 int check_error(int word);
