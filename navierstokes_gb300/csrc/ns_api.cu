@@ -332,7 +332,7 @@ int create_split(ns_ctx *c)
         (rc = dalloc(c, &sp.ycl, (size_t)ns::kCoefStride * jmax)) ||
         (rc = dalloc(c, &sp.sigx, (size_t)imax)) || (rc = dalloc(c, &sp.sigy, (size_t)jmax)) ||
         (rc = dalloc(c, &sp.rho_bc, (size_t)jmax)) || (rc = dalloc(c, &sp.ycorr, 4 * (size_t)jmax)) ||
-        (rc = dalloc(c, &sp.mean_buf, 4 * (size_t)jmax)) ||
+        (rc = dalloc(c, &sp.mean_buf, 5 * (size_t)jmax)) ||
         (rc = dalloc(c, &c->stage_sin, 8)) || (rc = dalloc(c, &c->d_iter, 1)) ||
         (rc = dalloc(c, &c->d_count, 1)) || (rc = dalloc(c, &c->d_err, 1)))
         return rc;
@@ -376,12 +376,13 @@ int create_split(ns_ctx *c)
     for (size_t q = 0; q < ty.size(); q++) tyl[q] = (float)(ty[q] - (double)tyf[q]);
     std::vector<float> sx(p->sigmax, p->sigmax + imax), sy(p->sigmay, p->sigmay + jmax);
     // base-flow quantities (FP64, rounded once)
-    std::vector<float> mean(4 * (size_t)jmax), rbc(jmax), corr(4 * (size_t)jmax, 0.f);
+    std::vector<float> mean(5 * (size_t)jmax), rbc(jmax), corr(4 * (size_t)jmax, 0.f);
     for (int j = 0; j < jmax; j++) {
         mean[j] = (float)rho[j];
         mean[jmax + j] = (float)uu[j];
         mean[2 * jmax + j] = (float)line_derivative(rho.data(), j, jmax, &ty[(size_t)j * ns::kCoefStride]);
         mean[3 * jmax + j] = (float)line_derivative(uu.data(), j, jmax, &ty[(size_t)j * ns::kCoefStride]);
+        mean[4 * jmax + j] = (float)(uu[j] - (double)mean[jmax + j]);
         rbc[j] = (float)(p->rhob[j] - rho[j]);
     }
     {
@@ -423,6 +424,7 @@ int create_split(ns_ctx *c)
     sp.mean.u = sp.mean_buf + jmax;
     sp.mean.drho = sp.mean_buf + 2 * jmax;
     sp.mean.du = sp.mean_buf + 3 * jmax;
+    sp.mean.ulo = sp.mean_buf + 4 * jmax;
     sp.mean.p = (float)pb;
     sp.mean.gamma = (float)p->gamma;
     sp.p_bc = 1.0 / p->gamma - pb;

@@ -22,6 +22,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "ns_check.cuh"
@@ -349,12 +350,20 @@ __device__ void stage_tile(const Args &a, int st, int4 item, const T *qin, T *qo
                 }
                 r[3] = -t;
                 double *Wp = a.W + in.w_off + idx;
+                // FP64 instances: w = alpha*w + dt*R, U += beta*w (rk.f90:163-164).
+                // FP32 perturbations carry w/dt instead (w~ = alpha*w~ + R,
+                // q' += (beta*dt)*w~), so that dt enters only through the FP64
+                // product beta*dt and not as FP32(dt)*R, whose rounding of dt
+                // would scale every step (ns_split.cu does the same).
+                constexpr bool kF32 = std::is_same<T, float>::value;
+                const double bw = kF32 ? a.beta[st] * in.dt_d : a.beta[st];
 #pragma unroll
                 for (int k = 0; k < 4; k++) {
-                    const double dr = to_d<T>(pick<T>(in.dt_f, in.dt_d) * r[k]);
+                    const double dr =
+                        kF32 ? to_d<T>(r[k]) : to_d<T>(pick<T>(in.dt_f, in.dt_d) * r[k]);
                     const double w = (st == 0) ? dr : fma(a.alpha[st], Wp[k * plane], dr);
-                    if (st < 5) Wp[k * plane] = w;  // stage 0 sets w = dt*R
-                    qv[k] = from_d<T>(fma(a.beta[st], w, to_d<T>(qv[k])));
+                    if (st < 5) Wp[k * plane] = w;  // stage 0 sets w (or w~)
+                    qv[k] = from_d<T>(fma(bw, w, to_d<T>(qv[k])));
                 }
             }
             if (j < in.D || j >= in.jmax - in.D) {

@@ -130,6 +130,7 @@ struct StageCoef {
 // rounded to FP32, and the constants.
 struct SplitMean {
     const float *rho, *u, *drho, *du;
+    const float *ulo;  // u_b - FP32(u_b) per row
     float p, gamma;
 };
 

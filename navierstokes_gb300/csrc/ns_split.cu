@@ -336,7 +336,7 @@ __global__ void __launch_bounds__(256, VISC ? 3 : kSplitMinBlocks)
                   const float *__restrict__ ycl, const SplitMean mean,
                   const float *__restrict__ sigx, const float *__restrict__ sigy,
                   const float *__restrict__ src, const double *__restrict__ stage_sin,
-                  float dt, double alpha, double beta, int stage)
+                  double alpha, double bdt, int stage)
 {
     constexpr int NPL = 4 + NP;
     __shared__ alignas(128) float sq[NPL][kSH][kSW];
@@ -396,10 +396,32 @@ __global__ void __launch_bounds__(256, VISC ? 3 : kSplitMinBlocks)
         const float *cyp = yc + kCoefStride * j;
         const bool yint = (j >= 3 && j < d.jmax - 3);
         const float *cylp = ycl + kCoefStride * j;
+        // With pairs, where the interior stencil applies in both directions
+        // (such a point is interior too): du'/dx, dv'/dx and dv'/dy of the
+        // hi planes in float-float (the differences exact, each coefficient
+        // as hi + lo, the products exact, the sum compensated), for the
+        // divergence and the base-flow advection below.
+        const bool ffp = NP >= 2 && xint && yint;
+        float uxh = 0.f, uxl = 0.f, vxh = 0.f, vxl = 0.f, vyh = 0.f, vyl = 0.f;
+        if (ffp) {
+            const float chx[3] = {cx4, cx5, cx6}, clx[3] = {clx4, clx5, clx6};
+            const float chy[3] = {cyp[4], cyp[5], cyp[6]}, cly[3] = {cylp[4], cylp[5], cylp[6]};
+            const float upx[3] = {sq[1][sr][sc + 1], sq[1][sr][sc + 2], sq[1][sr][sc + 3]};
+            const float umx[3] = {sq[1][sr][sc - 1], sq[1][sr][sc - 2], sq[1][sr][sc - 3]};
+            const float vpx[3] = {sq[2][sr][sc + 1], sq[2][sr][sc + 2], sq[2][sr][sc + 3]};
+            const float vmx[3] = {sq[2][sr][sc - 1], sq[2][sr][sc - 2], sq[2][sr][sc - 3]};
+            const float vpy[3] = {sq[2][sr + 1][sc], sq[2][sr + 2][sc], sq[2][sr + 3][sc]};
+            const float vmy[3] = {sq[2][sr - 1][sc], sq[2][sr - 2][sc], sq[2][sr - 3][sc]};
+            drp_ff(upx, umx, chx, clx, uxh, uxl);
+            drp_ff(vpx, vmx, chx, clx, vxh, vxl);
+            drp_ff(vpy, vmy, chy, cly, vyh, vyl);
+        }
 #pragma unroll
         for (int k = 0; k < NPL; k++) {
             q[k] = sq[k][sr][sc];
-            if (xint) {
+            if (ffp && (k == 1 || k == 2)) {
+                gx[k] = k == 1 ? uxh + uxl : vxh + vxl;
+            } else if (xint) {
                 const float d1 = sq[k][sr][sc + 1] - sq[k][sr][sc - 1];
                 const float d2 = sq[k][sr][sc + 2] - sq[k][sr][sc - 2];
                 const float d3 = sq[k][sr][sc + 3] - sq[k][sr][sc - 3];
@@ -411,7 +433,9 @@ __global__ void __launch_bounds__(256, VISC ? 3 : kSplitMinBlocks)
             } else {
                 gx[k] = closure_f32(qin + k * fplane + fidx, 1, i, d.imax, cxp);
             }
-            if (yint) {
+            if (ffp && k == 2) {
+                gy[k] = vyh + vyl;
+            } else if (yint) {
                 const float d1 = sq[k][sr + 1][sc] - sq[k][sr - 1][sc];
                 const float d2 = sq[k][sr + 2][sc] - sq[k][sr - 2][sc];
                 const float d3 = sq[k][sr + 3][sc] - sq[k][sr - 3][sc];
@@ -431,21 +455,42 @@ __global__ void __launch_bounds__(256, VISC ? 3 : kSplitMinBlocks)
             // O(|u'|) terms cancel, and a plain FP32 rounding of them would
             // be the same every stage and drive p' coherently.
             float div;
+            // U_b*du'/dx and U_b*dv'/dx (pairs only, interior stencil) as
+            // float-float (ah + al): at a vortex advected by the base flow
+            // these dominate the u' and v' right-hand sides, and their FP32
+            // rounding, different every stage, was the larger part of the
+            // error p' picks up there.
+            float ah[3] = {0.f, 0.f, 0.f}, al[3] = {0.f, 0.f, 0.f};
+            bool adv_ff = false;
             if (xint && yint) {
-                const float fpx[3] = {sq[1][sr][sc + 1], sq[1][sr][sc + 2], sq[1][sr][sc + 3]};
-                const float fmx[3] = {sq[1][sr][sc - 1], sq[1][sr][sc - 2], sq[1][sr][sc - 3]};
-                const float fpy[3] = {sq[2][sr + 1][sc], sq[2][sr + 2][sc], sq[2][sr + 3][sc]};
-                const float fmy[3] = {sq[2][sr - 1][sc], sq[2][sr - 2][sc], sq[2][sr - 3][sc]};
-                const float chx[3] = {cx4, cx5, cx6}, clx[3] = {clx4, clx5, clx6};
-                const float chy[3] = {cyp[4], cyp[5], cyp[6]},
-                            cly[3] = {cylp[4], cylp[5], cylp[6]};
-                float xh, xl, yh, yl, sh, se;
-                drp_ff(fpx, fmx, chx, clx, xh, xl);
-                drp_ff(fpy, fmy, chy, cly, yh, yl);
+                float xh = uxh, xl = uxl, yh = vyh, yl = vyl, sh, se;
+                if constexpr (NP < 2) {
+                    // single FP32 perturbations: the divergence's own
+                    // float-float derivatives
+                    const float fpx[3] = {sq[1][sr][sc + 1], sq[1][sr][sc + 2], sq[1][sr][sc + 3]};
+                    const float fmx[3] = {sq[1][sr][sc - 1], sq[1][sr][sc - 2], sq[1][sr][sc - 3]};
+                    const float fpy[3] = {sq[2][sr + 1][sc], sq[2][sr + 2][sc], sq[2][sr + 3][sc]};
+                    const float fmy[3] = {sq[2][sr - 1][sc], sq[2][sr - 2][sc], sq[2][sr - 3][sc]};
+                    const float chx[3] = {cx4, cx5, cx6}, clx[3] = {clx4, clx5, clx6};
+                    const float chy[3] = {cyp[4], cyp[5], cyp[6]},
+                                cly[3] = {cylp[4], cylp[5], cylp[6]};
+                    drp_ff(fpx, fmx, chx, clx, xh, xl);
+                    drp_ff(fpy, fmy, chy, cly, yh, yl);
+                }
                 two_sum(xh, yh, sh, se);
                 // the lo parts' derivatives are small: plain FP32 is exact enough
                 div = sh + (se + (xl + yl));
-                if (NP >= 2) div += gx[NP >= 2 ? 4 : 0] + gy[NP >= 2 ? 5 : 0];
+                if constexpr (NP >= 2) {
+                    div += gx[4] + gy[5];
+                    // U_b (hi + lo) times d/dx of the hi plane (float-float)
+                    // plus that of the lo plane, the product's rounding kept
+                    const float ub = mean.u[j], ubl = mean.ulo[j];
+                    ah[1] = ub * uxh;
+                    al[1] = fmaf(ub, uxh, -ah[1]) + fmaf(ub, uxl + gx[4], ubl * uxh);
+                    ah[2] = ub * vxh;
+                    al[2] = fmaf(ub, vxh, -ah[2]) + fmaf(ub, vxl + gx[5], ubl * vxh);
+                    adv_ff = true;
+                }
             } else {
                 div = gx[1] + gy[2];
                 if (NP >= 2) div += gx[NP >= 2 ? 4 : 0] + gy[NP >= 2 ? 5 : 0];
@@ -464,20 +509,39 @@ __global__ void __launch_bounds__(256, VISC ? 3 : kSplitMinBlocks)
             const float rhoy = mean.drho[j] + gy[0];
             const float uy = mean.du[j] + gy[1];
             const float ri = 1.0f / rho;
-            float r[4];
+            // r[k] + rl[k]: rl carries the float-float parts of u' and v'
+            float r[4], rl[4] = {0.f, 0.f, 0.f, 0.f};
             // rho*du/dx + rho*dv/dy (eqeuler.f90:63) as rho*div
             float t = uu * gx[0];
             t = fmaf(vv, rhoy, t);
             t = fmaf(rho, div, t);
             r[0] = -t;
-            t = uu * gx[1];
-            t = fmaf(ri, gx[3], t);
-            t = fmaf(vv, uy, t);
-            r[1] = -t;
-            t = uu * gx[2];
-            t = fmaf(vv, gy[2], t);
-            t = fmaf(ri, gy[3], t);
-            r[2] = -t;
+            if (adv_ff) {
+                // the other terms (u' d/dx, pressure gradient, v' d/dy) in FP32,
+                // summed with the advection pair
+                float t1 = q[1] * gx[1];
+                t1 = fmaf(ri, gx[3], t1);
+                t1 = fmaf(vv, uy, t1);
+                float t2 = q[1] * gx[2];
+                t2 = fmaf(vv, gy[2], t2);
+                t2 = fmaf(ri, gy[3], t2);
+                float rh, re;
+                two_sum(ah[1], al[1] + t1, rh, re);
+                r[1] = -rh;
+                rl[1] = -re;
+                two_sum(ah[2], al[2] + t2, rh, re);
+                r[2] = -rh;
+                rl[2] = -re;
+            } else {
+                t = uu * gx[1];
+                t = fmaf(ri, gx[3], t);
+                t = fmaf(vv, uy, t);
+                r[1] = -t;
+                t = uu * gx[2];
+                t = fmaf(vv, gy[2], t);
+                t = fmaf(ri, gy[3], t);
+                r[2] = -t;
+            }
             // gamma*p*du/dx + gamma*p*dv/dy (eqeuler.f90:80-82) as gamma*p*div
             const float gp = mean.gamma * pp;
             t = uu * gx[3];
@@ -508,8 +572,8 @@ __global__ void __launch_bounds__(256, VISC ? 3 : kSplitMinBlocks)
                     return rx + ry;
                 };
                 const float rv = vis.inv_re * ri;
-                r[1] = fmaf(rv, dxy(0, 1), r[1]);
-                r[2] = fmaf(rv, dxy(1, 2), r[2]);
+                rl[1] = fmaf(rv, dxy(0, 1), rl[1]);
+                rl[2] = fmaf(rv, dxy(1, 2), rl[2]);
                 const float t0 = sv[0][sr][sc], t1 = sv[1][sr][sc], t2 = sv[2][sr][sc];
                 float phi = gx[1] * t0;
                 phi = fmaf(gx[2], t1, phi);
@@ -518,23 +582,29 @@ __global__ void __launch_bounds__(256, VISC ? 3 : kSplitMinBlocks)
                 r[3] = fmaf(vis.gm1_re, phi, r[3]);
                 r[3] = fmaf(vis.inv_re_pr, dxy(3, 4), r[3]);
             }
-            // rk_steep (rk.f90:163-164): FP64 accumulator; u', v' kept as pairs
+            // rk_steep (rk.f90:163-164) with the FP64 accumulator carried as
+            // w/dt: w~ = alpha*w~ + R, q' += (beta*dt)*w~ (bdt).  R enters FP64
+            // exactly and dt only through the FP64 product beta*dt: an FP32
+            // dt*R would advance every stage by FP32(dt), whose relative
+            // error (up to 2^-24) shifts each wave's phase in proportion to
+            // the time run.  u', v' kept as pairs.
 #pragma unroll
             for (int k = 0; k < 4; k++) {
-                const double dr = f2d_exact(dt * r[k]);
+                double dr = f2d_exact(r[k]);
+                if (NP >= 2 && (k == 1 || k == 2)) dr += f2d_exact(rl[k]);
                 const double w = FIRST ? dr : fma(alpha, wold[h][k], dr);
-                // stage 5's w is never read: stage 0 sets w = dt*R
+                // stage 5's w is never read: stage 0 sets w~ = R
                 if (stage < 5) W[k * d.plane + didx] = w;
                 if (is_pair<NP>(k)) {
-                    // hi + beta*w in FP64, split exactly; the old lo joins in FP32
-                    // (both parts are below an FP32 ulp of hi)
+                    // hi + beta*dt*w~ in FP64, split exactly; the old lo joins in
+                    // FP32 (both parts are below an FP32 ulp of hi)
                     float &lo = q[is_pair<NP>(k) ? k + 3 : k];
                     float hi, rem;
-                    d2f_split(fma(beta, w, f2d_exact(q[k])), hi, rem);
+                    d2f_split(fma(bdt, w, f2d_exact(q[k])), hi, rem);
                     lo = rem + lo;
                     q[k] = hi;
                 } else {
-                    q[k] = d2f_rn(fma(beta, w, f2d_exact(q[k])));
+                    q[k] = d2f_rn(fma(bdt, w, f2d_exact(q[k])));
                 }
             }
         }
@@ -1123,7 +1193,7 @@ static cudaError_t launch_split_np(ns_ctx *c, int cls, int stage, cudaStream_t s
     k_split_stage<NP, FIRST, SRC, VISC><<<grd, blk, 0, s>>>(                                    \
         sp.qmap[stage & 1], sp.vmap, sp.tau, sp.trf, sp.vis, c->d_err, d, sp.fpitch, qa, qb,    \
         c->W, sp.xc, sp.yc, sp.xcl, sp.ycl, sp.mean, sp.sigx, sp.sigy, sp.src, c->stage_sin,    \
-        (float)c->p.dt, c->alpha[stage], c->beta[stage], stage)
+        c->alpha[stage], c->beta[stage] * c->p.dt, stage)
 #define NS_SPL2(VISC)                                                                           \
     if (stage == 0) {                                                                           \
         if (src) NS_SPL(true, true, VISC); else NS_SPL(true, false, VISC);                      \

@@ -77,7 +77,10 @@ def test_split_4096_squared_1000_steps(nslib):
     """The split-precision workload at full size: 4096x4096 Euler at M = 0.5,
     pulse 1e-4 and vortex 1e-3, NS_PREC_SPLIT against the FP64 path on the
     same GPU; p' relative L2 and max error <= 1e-5 at steps 100, 500 and
-    1000."""
+    1000, and within half of that: the margin that the FP64 product
+    beta*dt in the accumulator update and the float-float base-flow
+    advection give (3.4e-6 at step 1000; an FP32 dt*R and FP32 advection
+    left 9.0e-6)."""
     from navierstokes_gb300 import Solver
     c = cases.uniform_flow_case()
     assert (c.imax, c.jmax, c.steps) == (4096, 4096, 1000)
@@ -94,7 +97,7 @@ def test_split_4096_squared_1000_steps(nslib):
     for n in marks:
         l2, mx = p_errors(snaps[L.NS_PREC_SPLIT, n], snaps[L.NS_PREC_FP64, n], c.Ub)
         print(f"4096^2 split, step {n}: p' rel L2 {l2:.2e} max {mx:.2e}")
-        assert l2 <= TOL_PPRIME and mx <= TOL_PPRIME, (n, l2, mx)
+        assert l2 <= TOL_PPRIME / 2 and mx <= TOL_PPRIME / 2, (n, l2, mx)
 
 
 def test_split_with_source_and_chunked_filters(nslib):
