@@ -60,6 +60,7 @@ struct Args {
     const float *xcl, *ycl;
     const void *src;           // T*
     const double *stage_sin;   // [inst][8]
+    const double *bdt;         // [inst][6]: beta_k * dt, the FP32 instances' update factor
     double alpha[6], beta[6];
     // filter coefficients ([0] = x, [1] = y) in both precisions
     float fm_f[7], fbm1_f[2], fb_f[2][6], fbsum_f[2];
@@ -356,13 +357,14 @@ __device__ void stage_tile(const Args &a, int st, int4 item, const T *qin, T *qo
                 // product beta*dt and not as FP32(dt)*R, whose rounding of dt
                 // would scale every step (ns_split.cu does the same).
                 constexpr bool kF32 = std::is_same<T, float>::value;
-                const double bw = kF32 ? a.beta[st] * in.dt_d : a.beta[st];
 #pragma unroll
                 for (int k = 0; k < 4; k++) {
                     const double dr =
                         kF32 ? to_d<T>(r[k]) : to_d<T>(pick<T>(in.dt_f, in.dt_d) * r[k]);
                     const double w = (st == 0) ? dr : fma(a.alpha[st], Wp[k * plane], dr);
                     if (st < 5) Wp[k * plane] = w;  // stage 0 sets w (or w~)
+                    // beta*dt from the per-instance table, read where it is used
+                    const double bw = kF32 ? a.bdt[item.x * 6 + st] : a.beta[st];
                     qv[k] = from_d<T>(fma(bw, w, to_d<T>(qv[k])));
                 }
             }
@@ -826,7 +828,7 @@ struct ns_batch {
     std::vector<double> hpmean;
     size_t qsize = 0, wsize = 0;                  // elements
     void *q[2] = {nullptr, nullptr};
-    double *W = nullptr, *stage_sin = nullptr, *wf = nullptr, *dtv = nullptr;
+    double *W = nullptr, *stage_sin = nullptr, *wf = nullptr, *dtv = nullptr, *bdt = nullptr;
     double *drho = nullptr, *du = nullptr;        // FP64 per-row base flow for conversions
     double *stagebuf = nullptr;                   // FP64 staging planes for host transfers
     size_t stagebuf_elems = 0;
@@ -921,7 +923,7 @@ int bput(ns_batch *b, T *d, const std::vector<T> &v)
 void bfree(ns_batch *b)
 {
     if (b->exec) cudaGraphExecDestroy(b->exec);
-    void *ps[] = {b->q[0], b->q[1], b->W, b->stage_sin, b->wf, b->dtv, b->drho, b->du,
+    void *ps[] = {b->q[0], b->q[1], b->W, b->stage_sin, b->wf, b->dtv, b->bdt, b->drho, b->du,
                   b->stagebuf, b->inst, b->tiles[0], b->tiles[1], b->fx, b->fy, b->bc,
                   b->xc, b->xcl, b->yc, b->ycl, b->sigx, b->sigy, b->rho_bc, b->mrho, b->mu,
                   b->mdrho, b->mdu, b->corr, b->src, b->bar, b->err, b->d_iter, b->qmaps};
@@ -1100,7 +1102,7 @@ int ns_batch_create(const ns_params *const *params, int n, int precision, ns_bat
     std::vector<double> xcd, ycd;
     std::vector<double> xc, yc, sx, sy, rbc, mrho, mu, mdrho, mdu, corr;
     std::vector<float> xcl, ycl;
-    std::vector<double> rhoj, uj, wfv, dtv;
+    std::vector<double> rhoj, uj, wfv, dtv, bdtv;
     long long qoff = 0, woff = 0, soff = 0;
     int xoff = 0, yoff = 0;
     double sigmaf = params[0]->sigmaf;
@@ -1194,6 +1196,7 @@ int ns_batch_create(const ns_params *const *params, int n, int precision, ns_bat
         b->hpmean.push_back(pb);
         wfv.push_back(p->wf);
         dtv.push_back(p->dt);
+        for (int k = 0; k < 6; k++) bdtv.push_back(kBeta[k] * p->dt);
         xoff += imax;
         yoff += jmax;
     }
@@ -1262,6 +1265,7 @@ int ns_batch_create(const ns_params *const *params, int n, int precision, ns_bat
     B_TRY(balloc(b, &b->stage_sin, (size_t)8 * n));
     B_TRY(balloc(b, &b->wf, (size_t)n));
     B_TRY(balloc(b, &b->dtv, (size_t)n));
+    B_TRY(balloc(b, &b->bdt, (size_t)6 * n));
     B_TRY(balloc(b, &b->drho, rhoj.size()));
     B_TRY(balloc(b, &b->du, uj.size()));
     B_TRY(balloc(b, &b->stagebuf, b->stagebuf_elems));
@@ -1347,6 +1351,7 @@ int ns_batch_create(const ns_params *const *params, int n, int precision, ns_bat
     B_TRY(bput(b, b->du, uj));
     B_TRY(bput(b, b->wf, wfv));
     B_TRY(bput(b, b->dtv, dtv));
+    B_TRY(bput(b, b->bdt, bdtv));
     if (b->has_src) {
         // spatial source fields (rk.f90:188-189), in the state's precision
         for (int q = 0; q < n; q++) {
@@ -1401,6 +1406,7 @@ int ns_batch_create(const ns_params *const *params, int n, int precision, ns_bat
         a.mrho = b->mrho; a.mu = b->mu; a.mdrho = b->mdrho; a.mdu = b->mdu; a.corr = b->corr;
         a.src = b->src;
         a.stage_sin = b->stage_sin;
+        a.bdt = b->bdt;
         for (int k = 0; k < 6; k++) {
             a.alpha[k] = kAlpha[k];
             a.beta[k] = kBeta[k];
