@@ -27,6 +27,7 @@
 
 #include "ns_check.cuh"
 #include "ns_coef.h"
+#include "ns_f32conv.cuh"
 #include "ns_internal.cuh"
 #include "ns_tma.cuh"
 
@@ -95,16 +96,6 @@ __device__ __forceinline__ double to_d(T x);
 template <>
 __device__ __forceinline__ double to_d<double>(double x) { return x; }
 
-__device__ __forceinline__ double f2d_exact(float x)
-{
-    const unsigned b = __float_as_uint(x);
-    const unsigned e = (b >> 23) & 0xffu;
-    if ((b & 0x7fffffffu) == 0u) return __hiloint2double((int)(b & 0x80000000u), 0);
-    if (e == 0u || e == 0xffu) return (double)x;
-    const unsigned m = b & 0x7fffffu;
-    const unsigned hi = (b & 0x80000000u) | ((e + (1023u - 127u)) << 20) | (m >> 3);
-    return __hiloint2double((int)hi, (int)(m << 29));
-}
 template <>
 __device__ __forceinline__ double to_d<float>(float x) { return f2d_exact(x); }
 
@@ -113,21 +104,7 @@ __device__ __forceinline__ T from_d(double x);
 template <>
 __device__ __forceinline__ double from_d<double>(double x) { return x; }
 template <>
-__device__ __forceinline__ float from_d<float>(double x)
-{
-    const unsigned hi = (unsigned)__double2hiint(x);
-    const unsigned lo = (unsigned)__double2loint(x);
-    const unsigned e = (hi >> 20) & 0x7ffu;
-    if (e < 1023u - 126u || e > 1023u + 127u) {
-        if (((hi & 0x7fffffffu) | lo) == 0u) return __uint_as_float(hi & 0x80000000u);
-        return (float)x;
-    }
-    const unsigned top = ((hi & 0xfffffu) << 3) | (lo >> 29);
-    const unsigned rest = lo & 0x1fffffffu;
-    unsigned f = (hi & 0x80000000u) | ((e - (1023u - 127u)) << 23) | top;
-    if (rest > (1u << 28) || (rest == (1u << 28) && (top & 1u))) f += 1u;
-    return __uint_as_float(f);
-}
+__device__ __forceinline__ float from_d<float>(double x) { return d2f_rn(x); }
 
 // Grid-wide barrier with a bounded wait.  Returns false when this or another
 // block gave up (the error word is set), after which callers return.

@@ -23,79 +23,14 @@
 // 3 p' (hi parts), then 3 + k the lo part of variable k = 1 .. NP.
 //
 // FP64 <-> FP32 conversions of the accumulator update are done with integer
-// bit operations (IEEE-754 layouts, round to nearest even): on GB300 the F2F
-// instructions run on the FP64 pipe, which is about 60x slower than FP32.
+// bit operations (ns_f32conv.cuh): on GB300 the F2F instructions run on the
+// FP64 pipe, which is about 60x slower than FP32.
 #include "ns_internal.cuh"
 #include "ns_check.cuh"
+#include "ns_f32conv.cuh"
 #include "ns_tma.cuh"
 
 namespace ns {
-
-// ---------------------------------------------------------------------------
-// Exact conversions on the integer pipe
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ double f2d_exact(float x)
-{
-    const unsigned b = __float_as_uint(x);
-    const unsigned e = (b >> 23) & 0xffu;
-    if ((b & 0x7fffffffu) == 0u) return __hiloint2double((int)(b & 0x80000000u), 0);  // +-0
-    if (e == 0u || e == 0xffu) return (double)x;  // subnormal, inf, nan
-    const unsigned m = b & 0x7fffffu;
-    const unsigned hi = (b & 0x80000000u) | ((e + (1023u - 127u)) << 20) | (m >> 3);
-    const unsigned lo = m << 29;
-    return __hiloint2double((int)hi, (int)lo);
-}
-
-__device__ __forceinline__ float d2f_rn(double x)
-{
-    const unsigned hi = (unsigned)__double2hiint(x);
-    const unsigned lo = (unsigned)__double2loint(x);
-    const unsigned e = (hi >> 20) & 0x7ffu;
-    // normal FP32 results only (exponent 2^-126 .. 2^127); the rest is rare
-    if (e < 1023u - 126u || e > 1023u + 127u) {
-        if (((hi & 0x7fffffffu) | lo) == 0u) return __uint_as_float(hi & 0x80000000u);
-        return (float)x;
-    }
-    const unsigned top = ((hi & 0xfffffu) << 3) | (lo >> 29);  // 23 mantissa bits
-    const unsigned rest = lo & 0x1fffffffu;                    // 29 discarded bits
-    unsigned f = (hi & 0x80000000u) | ((e - (1023u - 127u)) << 23) | top;
-    const unsigned half = 1u << 28;
-    if (rest > half || (rest == half && (top & 1u))) f += 1u;  // carry may bump the exponent
-    return __uint_as_float(f);
-}
-
-// hi = x rounded to FP32 (nearest even) and lo = x - hi rounded to FP32, with
-// integer operations and one integer-to-float conversion, no FP64-pipe
-// instruction: the remainder is the 29 discarded mantissa bits, minus 2^29
-// when hi rounded up, times 2^(e - 1075).  Zero, |x| < 2^-74 and |x| >= 2^128
-// take the plain conversions.
-__device__ __forceinline__ void d2f_split(double x, float &hi, float &lo)
-{
-    const unsigned xh = (unsigned)__double2hiint(x), xl = (unsigned)__double2loint(x);
-    const unsigned e = (xh >> 20) & 0x7ffu;
-    if (((xh & 0x7fffffffu) | xl) == 0u) {
-        hi = __uint_as_float(xh & 0x80000000u);
-        lo = 0.f;
-        return;
-    }
-    if (e < 949u || e > 1150u) {
-        hi = d2f_rn(x);
-        lo = d2f_rn(x - f2d_exact(hi));
-        return;
-    }
-    const unsigned top = ((xh & 0xfffffu) << 3) | (xl >> 29);  // 23 mantissa bits
-    const unsigned rest = xl & 0x1fffffffu;                    // 29 discarded bits
-    unsigned f = (xh & 0x80000000u) | ((e - 896u) << 23) | top;
-    int r = (int)rest;
-    const unsigned half = 1u << 28;
-    if (rest > half || (rest == half && (top & 1u))) {  // carry may bump the exponent
-        f += 1u;
-        r -= (1 << 29);
-    }
-    hi = __uint_as_float(f);
-    const float mag = __int2float_rn(r) * __uint_as_float((e - 948u) << 23);
-    lo = (xh & 0x80000000u) ? -mag : mag;
-}
 
 // ---------------------------------------------------------------------------
 // Fused stage kernel: FP32 derivatives from a shared-memory tile, Euler RHS,
@@ -325,8 +260,13 @@ __global__ void __launch_bounds__(256, kSplitMinBlocks)
     }
 }
 
+// Resident blocks per SM: 4 with pairs (64 registers), 5 with single FP32
+// perturbations (48 registers), 3 with the viscous tile.
+template <int NP, bool VISC>
+constexpr int split_stage_blocks() { return VISC ? 3 : (NP == 0 ? 5 : kSplitMinBlocks); }
+
 template <int NP, bool FIRST, bool SRC, bool VISC>
-__global__ void __launch_bounds__(256, VISC ? 3 : kSplitMinBlocks)
+__global__ void __launch_bounds__(256, split_stage_blocks<NP, VISC>())
     k_split_stage(const __grid_constant__ CUtensorMap qmap, const __grid_constant__ CUtensorMap vmap,
                   const float *__restrict__ tau, const float *__restrict__ trf, const SplitVisc vis,
                   int *__restrict__ err, Dims d,
