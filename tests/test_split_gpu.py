@@ -79,7 +79,7 @@ def test_split_4096_squared_1000_steps(nslib):
     same GPU; p' relative L2 and max error <= 1e-5 at steps 100, 500 and
     1000, and within half of that: the margin that the FP64 product
     beta*dt in the accumulator update and the float-float base-flow
-    advection give (3.4e-6 at step 1000; an FP32 dt*R and FP32 advection
+    advection give (3.9e-6 at step 1000; an FP32 dt*R and FP32 advection
     left 9.0e-6)."""
     from navierstokes_gb300 import Solver
     c = cases.uniform_flow_case()
