@@ -47,19 +47,19 @@ BYTES_PER_POINT = {"k_prim": 32, "k_first": 144, "k_update": 240, "k_filter_x": 
 # per DFMA, 1 per DADD/DMUL) and FP64-pipe thread instructions (DFMA, DADD,
 # DMUL and the FP32<->FP64 conversions, which share that pipe on GB300).
 FP64_FLOP_PER_POINT = {"k_prim": 12.0, "k_first": 113.15, "k_update": 111.43,
-                       "k_filter_x": 90.15, "k_filter_y": 90.15}
+                       "k_filter_x": 82.44, "k_filter_y": 82.44}
 FP64_INST_PER_POINT = {"k_prim": 7.0, "k_first": 81.03, "k_update": 71.84,
-                       "k_filter_x": 58.56, "k_filter_y": 58.56}
+                       "k_filter_x": 53.78, "k_filter_y": 53.78}
 # DRAM bytes (read + write) per point of one launch from the same capture
 # (2048x2048), scaled to a launch by the number of points.
 TRAFFIC_PER_POINT = {"k_prim": 21.3, "k_first": 129.9, "k_update": 230.5,
-                     "k_filter_x": 61.7, "k_filter_y": 61.7}
+                     "k_filter_x": 56.6, "k_filter_y": 56.0}
 # DFMA throughput of a register-only loop measured on a GB300 (1.68 DFMA per
 # clock per SM at 2.07 GHz), used when ns_fp64_peak() cannot run
 FP64_PEAK_FALLBACK_TFLOPS = 1.19
 # FP64-pipe thread instructions per point-step of the whole step (sum of the
 # per-launch counts above over the step's 36 launches, nk = 4)
-FP64_INST_PER_POINT_STEP = 1662
+FP64_INST_PER_POINT_STEP = 1605
 STEP_BYTES_FUSED_MIN = 1536  # compulsory bytes per point-step of a fused FP64 design, nk = 4
 
 
