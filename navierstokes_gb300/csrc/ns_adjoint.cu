@@ -542,7 +542,9 @@ struct ns_adjoint {
     // 4 planes for the state after the segment's last step; segment sg uses
     // store2 when sg is odd and store2 exists (recompute beside reverse)
     double *store = nullptr, *store2 = nullptr;
-    bool last_seg_stored = false;  // the forward kept the last segment's stages
+    // segments at the end of the run whose stages the forward kept in their
+    // stores (0, 1, or 2 when the second store exists)
+    int stored_segs = 0;
     cudaStream_t s_rec = nullptr, s_rev = nullptr;
     cudaEvent_t ev_rec[2] = {}, ev_rev[2] = {}, ev_start = nullptr;
     // K = 0: every stage's input of every step kept (nsteps x 6 x 4 planes)
@@ -905,18 +907,26 @@ int ns_adjoint_forward(ns_adjoint *a, const double *U0, int layout, int iter0, i
         A_CUDA(a, cudaMalloc(&a->chk, (size_t)nchk * 4 * P * sizeof(double)));
         a->nchk = nchk;
     }
-    // the last segment's steps keep their stage inputs and derivatives (the
-    // reverse pass starts there without recomputing it); the rest replay the
-    // step graph
+    // The steps of the last segment, and of the one before it when the
+    // second store exists, keep their stage inputs and derivatives in the
+    // stores the reverse pass reads them from (it starts without recomputing
+    // either); the rest replay the step graph.
     const int last0 = (nchk - 1) * K;
     double *last = seg_store(a, nchk - 1);
+    const bool keep_prev = a->store2 && nchk >= 2;
+    const int prev0 = keep_prev ? (nchk - 2) * K : last0;
+    double *prev = keep_prev ? seg_store(a, nchk - 2) : nullptr;
     A_CUDA(a, cudaMemsetAsync(a->loss, 0, sizeof(double), s));
     for (int n = 0; n < nsteps; n++) {
         if (n % K == 0)
             A_CUDA(a, cudaMemcpyAsync(a->chk + (size_t)(n / K) * 4 * P, c->U, 4 * P * sizeof(double),
                                       cudaMemcpyDeviceToDevice, s));
-        rc = (n >= last0) ? forward_step(a, iter0 + n, seg_slot(last, n - last0, P), s)
-                          : ns_step(c, iter0 + n, 1);
+        if (keep_prev && n == last0)  // the state after the previous segment's last step
+            A_CUDA(a, cudaMemcpyAsync(seg_slot(prev, K, P), c->U, 4 * P * sizeof(double),
+                                      cudaMemcpyDeviceToDevice, s));
+        rc = (n >= last0)   ? forward_step(a, iter0 + n, seg_slot(last, n - last0, P), s)
+             : (n >= prev0) ? forward_step(a, iter0 + n, seg_slot(prev, n - prev0, P), s)
+                            : ns_step(c, iter0 + n, 1);
         if (rc != NS_OK) return rc;
         ns::adj::k_obs_loss<<<1, 32, 0, s>>>(c->U, c->d, a->obs, a->nobs, a->pb, a->loss);
     }
@@ -928,7 +938,7 @@ int ns_adjoint_forward(ns_adjoint *a, const double *U0, int layout, int iter0, i
     a->nsteps = nsteps;
     a->iter0 = iter0;
     a->forward_done = true;
-    a->last_seg_stored = true;
+    a->stored_segs = keep_prev ? 2 : 1;
     return NS_OK;
 }
 
@@ -1036,8 +1046,10 @@ int ns_adjoint_backward(ns_adjoint *a, double *grad_field)
     do {                                   \
         if ((rc = (call)) != NS_OK) return rc; \
     } while (0)
+    // segments sg >= kept need no recompute: the forward left them in place
+    const int kept = nseg - std::min(a->stored_segs, nseg);
     if (nseg > 0) {
-        if (a->last_seg_stored) {
+        if (nseg - 1 >= kept) {
             A_CUDA(a, cudaEventRecord(a->ev_rec[(nseg - 1) & 1], srec));
         } else {
             A_TRY(rec_begin(nseg - 1));
@@ -1046,16 +1058,20 @@ int ns_adjoint_backward(ns_adjoint *a, double *grad_field)
         }
     }
     // the stores are reused below: a second backward recomputes every segment
-    a->last_seg_stored = false;
+    a->stored_segs = 0;
     for (int sg = nseg - 1; sg >= 0; sg--) {
         A_CUDA(a, cudaStreamWaitEvent(srev, a->ev_rec[sg & 1], 0));
         const int nr = seg_len(sg), n1 = seg_n0(sg) + nr;
-        const int nc = sg > 0 ? seg_len(sg - 1) : 0;
+        // segment sg-1 is recomputed unless the forward kept it
+        const bool rec = sg > 0 && sg - 1 < kept;
+        const int nc = rec ? seg_len(sg - 1) : 0;
         if (pipe) {
-            if (sg > 0) {
+            if (rec) {
                 // segment sg-1 goes into the store segment sg+1 was reversed from
                 if (sg + 1 < nseg) A_CUDA(a, cudaStreamWaitEvent(srec, a->ev_rev[(sg + 1) & 1], 0));
                 A_TRY(rec_begin(sg - 1));
+            } else if (sg > 0) {
+                A_CUDA(a, cudaEventRecord(a->ev_rec[(sg - 1) & 1], srec));
             }
             // one step of each chain at a time, so that neither stream's
             // queue runs ahead of the other's
@@ -1063,7 +1079,7 @@ int ns_adjoint_backward(ns_adjoint *a, double *grad_field)
                 if (q < nr) A_TRY(rev_step(sg, n1 - 1 - q));
                 if (q < nc) A_TRY(rec_step(sg - 1, q));
             }
-            if (sg > 0) A_TRY(rec_end(sg - 1));
+            if (rec) A_TRY(rec_end(sg - 1));
             A_CUDA(a, cudaEventRecord(a->ev_rev[sg & 1], srev));
         } else {
             for (int q = 0; q < nr; q++) A_TRY(rev_step(sg, n1 - 1 - q));
