@@ -13,10 +13,11 @@
 // and metrics (diff.f90:6-350).  The forward state is checkpointed every K
 // steps; each K-step segment is recomputed once, keeping every stage's input
 // state and derivatives, so the reverse pass recomputes nothing.  The
-// forward keeps the last segment's stage inputs itself, and the recompute of
-// segment s-1 runs on a second stream beside the reverse of segment s (two
-// segment stores): on grids of a few hundred thousand points one kernel
-// leaves much of the GPU idle, and the two chains are independent.
+// recompute of segment s-1 runs on a second stream beside the reverse of
+// segment s (two segment stores): on grids of a few hundred thousand points
+// one kernel leaves much of the GPU idle, and the two chains are
+// independent.  The forward keeps the stage inputs of the last two segments
+// in those stores itself (the last one only, without a second store).
 #include <algorithm>
 #include <cmath>
 #include <string>
