@@ -474,10 +474,12 @@ __device__ __forceinline__ double dtrans(const double *__restrict__ g, long long
     return r;
 }
 
-// Block and tiles of k_deriv_t: 32 x 8 points; lx with its x halo (box
-// 40 x 8 x 4 from (i0-4, j0): the x coordinate times 8 bytes stays a
-// multiple of 16) and ly with its y halo (box 32 x 14 x 4 from (i0, j0-3)).
-constexpr int kDtBX = 32, kDtBY = 8, kDtXW = 40, kDtXL = 4, kDtYH = kDtBY + 6;
+// Block and tiles of k_deriv_t: 32 x 4 points; lx with its x halo (box
+// 40 x 4 x 4 from (i0-4, j0): the x coordinate times 8 bytes stays a
+// multiple of 16) and ly with its y halo (box 32 x 10 x 4 from (i0, j0-3)).
+// Small blocks (as k_point_t's) leave room beside them for the kernels of
+// the recompute stream: 32 x 8 blocks made the reverse pass 2 % slower.
+constexpr int kDtBX = 32, kDtBY = 4, kDtXW = 40, kDtXL = 4, kDtYH = kDtBY + 6;
 
 // lam += Dx^T lx + Dy^T ly.  With TMA both tiles arrive in shared memory by
 // one bulk copy each and the interior gathers read them there; points within
@@ -674,7 +676,7 @@ int stage_adjoint(ns_adjoint *a, const double *U, const double *Um, const double
         ns::adj::k_filter_t<false><<<nb, 128, 0, s>>>(d, a->lam2, a->lam, seg, a->warm_t,
                                                        a->warm32_t, c->fx);
     }
-    const dim3 blk(32, 8), grd((d.imax + 31) / 32, (d.jmax + 7) / 8);
+    const dim3 blk(32, 4), grd((d.imax + 31) / 32, (d.jmax + 3) / 4);
     ns::adj::k_point_t<<<grd, blk, 0, s>>>(d, a->lam, a->om, a->lx, a->ly, U, Um, Un,
                                            c->sigx, c->sigy, a->gS, c->phys.gamma, c->p.dt,
                                            c->alpha[stage], c->beta[stage], sink);
