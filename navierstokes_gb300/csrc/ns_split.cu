@@ -18,7 +18,10 @@
 // stage; that noise random-walks at wavenumbers the selective filter does not
 // damp.  For a vortex with |u'| ~ 1e-3 next to an acoustic pulse it reached
 // ~35 ulps of u' after 300 steps and drove p' through the divergence to
-// 7e-10 (1e-4 of p'); the p' storage noise itself is the next floor (4e-11
+// 7e-10 (1e-4 of p').  With pairs the floor is the rounding of the FP32
+// right-hand side, which the base-flow advection in float-float and the
+// accumulator update by the FP64 product beta*dt keep near what an FP64
+// right-hand side from the same pairs gives (about 1e-11 of p' at the vortex
 // after 1000 steps).  Planes of a perturbation buffer: 0 rho', 1 u', 2 v',
 // 3 p' (hi parts), then 3 + k the lo part of variable k = 1 .. NP.
 //
